@@ -1,0 +1,153 @@
+/*
+ * pfast_gb300.h -- C ABI of the GB300 (sm_103a) implementation of PFAST's
+ * traveltime-and-gradient hot path: the Godunov fast-sweeping Eikonal solver,
+ * the Huygens reflection traveltime (2D) and the adjoint-state sweeps with
+ * per-source gradient accumulation.
+ *
+ * Plain C types only: pointers, sizes, doubles.  Every call returns a status
+ * code (PFAST_OK == 0); on failure pfast_last_error() holds a message.  No call
+ * exits the process.
+ *
+ * Index conventions are the reference's:
+ *   3D field  U[k*nrows*ncols + i*ncols + j]   k = z (dz), i = row (y, dy), j = col (x, dx)
+ *   2D field  U[i*ncols + j]                   i = row (depth, dz), j = col (x, dx)
+ *   3D src / rec / nxyz rows: 3 entries (row, col, z) / (n_y, n_x, n_z)
+ *   2D src / rec / nxy rows:  2 entries (row, col) / (n_z, n_x)
+ *   receiver rows of source s start at sum(srnum[0..s-1]).
+ */
+#ifndef PFAST_GB300_H
+#define PFAST_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int pfast_status;
+
+#define PFAST_OK 0
+#define PFAST_ERR_INVALID 1              /* bad argument: size, index, null pointer */
+#define PFAST_ERR_CUDA 2                 /* a CUDA runtime call failed */
+#define PFAST_ERR_NOMEM 3                /* device memory exhausted */
+#define PFAST_ERR_NO_DEVICE 4            /* no usable CUDA device */
+#define PFAST_ERR_NO_REFLECTION_POINT 5  /* no node above a reflector (src/RT_pfsm2d.h:232,257,281) */
+#define PFAST_ERR_NEGATIVE_TIME 6        /* reflected time < 0 (src/RT_pfsm2d.h:225-227,253,274) */
+
+/* Arithmetic of the sweeps. */
+#define PFAST_PLAIN_FP64 0   /* reference arithmetic in FP64, bit-identical with FMA contraction off */
+#define PFAST_MIXED 1        /* FP32 bulk sweeps, then FP64 polish sweeps until the FP64 test passes */
+
+typedef struct pfast_ctx pfast_ctx;
+typedef struct pfast_survey3d pfast_survey3d;
+typedef struct pfast_survey2d pfast_survey2d;
+
+typedef struct {
+    int precision;   /* PFAST_PLAIN_FP64 or PFAST_MIXED */
+    int maxswp;      /* MAXSwp: outer-iteration cap per solve (3D driver 100, 2D driver 500) */
+    int max_batch;   /* sources per device batch; 0 = as many as fit */
+} pfast_options;
+
+typedef struct {
+    long long fwd_node_updates;   /* executed node updates, forward sweeps (all precisions) */
+    long long adj_node_updates;   /* executed node updates, adjoint sweeps */
+    long long fwd64_node_updates; /* of which FP64 */
+    long long adj64_node_updates;
+    int fwd_iters_max;            /* largest FP64 outer-iteration count over the solves */
+    int adj_iters_max;
+    int fwd32_iters_max;          /* largest FP32 outer-iteration count (mixed mode) */
+    int adj32_iters_max;
+    int not_converged;            /* solves that stopped at maxswp */
+    int batches;                  /* device batches used */
+    long long launches;           /* kernels launched */
+    double ms_fwd32, ms_fwd64;    /* device time per phase, CUDA events on the context stream */
+    double ms_adj32, ms_adj64;
+    double ms_other;              /* initialisation, receiver conditions, gradient sums */
+    double ms_total;
+} pfast_stats;
+
+/* ------------------------------------------------------------------ library */
+const char* pfast_version(void);
+const char* pfast_status_string(pfast_status s);
+const char* pfast_last_error(void);          /* message of the last failure on this thread */
+void pfast_default_options(pfast_options* opt);
+
+pfast_status pfast_ctx_create(int device, pfast_ctx** out);
+pfast_status pfast_ctx_destroy(pfast_ctx* ctx);
+/* Run subsequent work on `stream` (a cudaStream_t); NULL restores the context's own stream. */
+pfast_status pfast_ctx_set_stream(pfast_ctx* ctx, void* stream);
+pfast_status pfast_ctx_synchronize(pfast_ctx* ctx);
+
+/* ---------------------------------------------- reference-signature entry points
+ * Same argument order and meaning as the reference functions; host buffers; a
+ * process-wide context on the current device.  `pe` is accepted and ignored
+ * (rank id, used only in the reference's messages).  Output arrays are fully
+ * overwritten, as in the reference.
+ */
+/* replaces fsm3d, src/T_pfsm3d.h:131 */
+pfast_status pfast_fsm3d(double* vp, double* U, int* src, int srcid, int MAXSwp, double dx, double dy,
+                         double dz, int nrows, int ncols, int nz, int pe);
+/* replaces adjoint_fsm3d, src/T_padjoint3d.h:73 (the misfit EE is returned in *EE) */
+pfast_status pfast_adjoint_fsm3d(double* U, double* T, double* T_obs, int* rec, double* nxyz, int* src,
+                                 int* srnum, int srcid, int MAXSwp, double dx, double dy, double dz,
+                                 int nrows, int ncols, int nz, int pe, double* EE);
+/* replaces RT_fsm2d, src/RT_pfsm2d.h:116 (rec and srnum are unused there, as in the reference) */
+pfast_status pfast_RT_fsm2d(double* vp, double* U, double* TTd, double* TTu, double* Z, int* src, int* rec,
+                            int* srnum, int srcid, int NumofR, int MAXSwp, double dx, double dz, int nrows,
+                            int ncols, int pe);
+/* replaces Tadjoint_fsm2d (Cr = 1 overload), src/RT_padjoint2d.h:288 */
+pfast_status pfast_Tadjoint_fsm2d(double* U, double* T, double* T_obs, int* rec, double* nxyz, int* src,
+                                  int* srnum, int srcid, int MAXSwp, double dx, double dz, int nrows, int ncols,
+                                  int pe, double* EE);
+/* replaces Radjoint_fsm2d (Cr = 1 overload), src/RT_padjoint2d.h:382 */
+pfast_status pfast_Radjoint_fsm2d(double* UR, double* Td, double* Tu, double* TR_obs, int* rec, double* nxyz,
+                                  int* src, int* srnum, int srcid, int NumofR, int MAXSwp, double dx, double dz,
+                                  int nrows, int ncols, int pe, double* EE);
+
+/* ------------------------------------------------------------ batched surveys
+ * A survey holds the acquisition geometry and picks on the device; evaluations
+ * then take the model.  This is the per-source loop of the drivers
+ * (src/T_PFAST3D.cpp:387-399, src/RT_PFAST2D.cpp:420-457) run as one batch on
+ * one GPU: the gradient is summed in source order, so the result equals the
+ * reference's single-process (np=1) result.
+ */
+/* 3D: src[nsrc*3], srnum[nsrc], rec[nrec*3], nxyz[nrec*3], T_obs[nrec]; host arrays, copied. */
+pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz, double dx, double dy,
+                                   double dz, int nsrc, const int* src, const int* srnum, const int* rec,
+                                   const double* nxyz, const double* T_obs, pfast_survey3d** out);
+pfast_status pfast_survey3d_destroy(pfast_survey3d* sv);
+/* Misfit + gradient (T_PFAST3D.cpp:387-399).  vp, grad: DEVICE arrays [nz*nrows*ncols]. */
+pfast_status pfast_survey3d_eval(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
+                                 double* grad, double* misfit, pfast_stats* stats);
+/* First-arrival picks (T_PFAST3D.cpp:672-686).  vp, picks: DEVICE arrays; picks[nrec]. */
+pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp,
+                                    const pfast_options* opt, double* picks, pfast_stats* stats);
+
+/* One-call host-buffer forms (copies in and out inside the call). */
+pfast_status pfast_eval3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy,
+                          double dz, int nsrc, const int* src, const int* srnum, const int* rec, const double* nxyz,
+                          const double* T_obs, const pfast_options* opt, double* grad, double* misfit,
+                          pfast_stats* stats);
+pfast_status pfast_forward3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy,
+                             double dz, int nsrc, const int* src, const int* srnum, const int* rec,
+                             const pfast_options* opt, double* picks, pfast_stats* stats);
+
+/* 2D: src[nsrc*2], srnum[nsrc], rec[nrec*2], nxy[nrec*2], TT_obs[nrec], TR_obs[nrec*NumofR],
+ * Z[NumofR*ncols*3] = (depth, n_z, n_x) per column.  nxy, TT_obs, TR_obs may be NULL for forward-only use. */
+pfast_status pfast_survey2d_create(pfast_ctx* ctx, int nrows, int ncols, double dx, double dz, int nsrc,
+                                   const int* src, const int* srnum, int nrec, const int* rec, const double* nxy,
+                                   const double* TT_obs, int NumofR, const double* TR_obs, const double* Z,
+                                   pfast_survey2d** out);
+pfast_status pfast_survey2d_destroy(pfast_survey2d* sv);
+/* Picks Tr[nrec*(NumofR+1)] (src/RT_PFAST2D.cpp:832-852).  vp, Tr: DEVICE arrays. */
+pfast_status pfast_survey2d_forward(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp,
+                                    const pfast_options* opt, double* Tr, pfast_stats* stats);
+/* Joint gradient (src/RT_PFAST2D.cpp:420-457): gT, gR, gRT = gT*(1-WR)+gR*WR, and the
+ * transmission / reflection misfits.  vp, WR, gT, gR, gRT: DEVICE arrays [nrows*ncols]. */
+pfast_status pfast_survey2d_eval(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, const double* WR,
+                                 const pfast_options* opt, double* gT, double* gR, double* gRT, double* Et,
+                                 double* Er, pfast_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFAST_GB300_H */

@@ -1,0 +1,103 @@
+"""ctypes binding of libpfast_gb300.so (the C ABI declared in include/pfast_gb300.h).
+
+The library is the only compute path: if it has not been built this module
+raises at import, there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpfast_gb300.so")
+
+PFAST_OK = 0
+PFAST_ERR_INVALID = 1
+PFAST_ERR_CUDA = 2
+PFAST_ERR_NOMEM = 3
+PFAST_ERR_NO_DEVICE = 4
+PFAST_ERR_NO_REFLECTION_POINT = 5
+PFAST_ERR_NEGATIVE_TIME = 6
+
+PFAST_PLAIN_FP64 = 0
+PFAST_MIXED = 1
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("fwd_node_updates", C.c_longlong), ("adj_node_updates", C.c_longlong),
+        ("fwd64_node_updates", C.c_longlong), ("adj64_node_updates", C.c_longlong),
+        ("fwd_iters_max", C.c_int), ("adj_iters_max", C.c_int),
+        ("fwd32_iters_max", C.c_int), ("adj32_iters_max", C.c_int),
+        ("not_converged", C.c_int), ("batches", C.c_int),
+        ("launches", C.c_longlong),
+        ("ms_fwd32", C.c_double), ("ms_fwd64", C.c_double),
+        ("ms_adj32", C.c_double), ("ms_adj64", C.c_double),
+        ("ms_other", C.c_double), ("ms_total", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# (name, restype, argtypes) of every entry point in include/pfast_gb300.h
+_p, _i, _d = C.c_void_p, C.c_int, C.c_double
+SIGNATURES = [
+    ("pfast_version", C.c_char_p, []),
+    ("pfast_status_string", C.c_char_p, [_i]),
+    ("pfast_last_error", C.c_char_p, []),
+    ("pfast_default_options", None, [_p]),
+    ("pfast_ctx_create", _i, [_i, _p]),
+    ("pfast_ctx_destroy", _i, [_p]),
+    ("pfast_ctx_set_stream", _i, [_p, _p]),
+    ("pfast_ctx_synchronize", _i, [_p]),
+    ("pfast_fsm3d", _i, [_p, _p, _p, _i, _i, _d, _d, _d, _i, _i, _i, _i]),
+    ("pfast_adjoint_fsm3d", _i, [_p, _p, _p, _p, _p, _p, _p, _i, _i, _d, _d, _d, _i, _i, _i, _i, _p]),
+    ("pfast_RT_fsm2d", _i, [_p, _p, _p, _p, _p, _p, _p, _p, _i, _i, _i, _d, _d, _i, _i, _i]),
+    ("pfast_Tadjoint_fsm2d", _i, [_p, _p, _p, _p, _p, _p, _p, _i, _i, _d, _d, _i, _i, _i, _p]),
+    ("pfast_Radjoint_fsm2d", _i, [_p, _p, _p, _p, _p, _p, _p, _p, _i, _i, _i, _d, _d, _i, _i, _i, _p]),
+    ("pfast_survey3d_create", _i, [_p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p]),
+    ("pfast_survey3d_destroy", _i, [_p]),
+    ("pfast_survey3d_eval", _i, [_p, _p, _p, _p, _p, _p, _p]),
+    ("pfast_survey3d_forward", _i, [_p, _p, _p, _p, _p, _p]),
+    ("pfast_eval3d", _i, [_p, _p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+    ("pfast_forward3d", _i, [_p, _p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p]),
+    ("pfast_survey2d_create", _i, [_p, _i, _i, _d, _d, _i, _p, _p, _i, _p, _p, _p, _i, _p, _p, _p]),
+    ("pfast_survey2d_destroy", _i, [_p]),
+    ("pfast_survey2d_forward", _i, [_p, _p, _p, _p, _p, _p]),
+    ("pfast_survey2d_eval", _i, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+]
+
+_lib = None
+
+
+def lib():
+    """The loaded library (raises if it was never built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"pfast_gb300 CUDA library missing at {LIB_PATH}: build it with "
+                              "`python -c 'import __graft_entry__ as g; g.build()'` (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class PfastError(RuntimeError):
+    def __init__(self, status, where=""):
+        L = lib()
+        msg = L.pfast_last_error().decode(errors="replace")
+        name = L.pfast_status_string(status).decode(errors="replace")
+        super().__init__(f"{where}: {name} (status {status}): {msg}")
+        self.status = status
+
+
+def check(status, where=""):
+    if status != PFAST_OK:
+        raise PfastError(status, where)

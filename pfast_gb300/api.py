@@ -1,0 +1,301 @@
+"""Python host side of pfast_gb300.
+
+Two layers, both over the C ABI (include/pfast_gb300.h):
+
+* Reference-signature functions with the reference's names, argument order and
+  in-place outputs on numpy host arrays: fsm3d (src/T_pfsm3d.h:131),
+  adjoint_fsm3d (src/T_padjoint3d.h:73), RT_fsm2d (src/RT_pfsm2d.h:116),
+  Tadjoint_fsm2d (src/RT_padjoint2d.h:288), Radjoint_fsm2d
+  (src/RT_padjoint2d.h:382).  Where the reference exits the process, these raise
+  PfastError.  The adjoint functions return the misfit EE, as the reference does.
+* Batched surveys (Survey3D / Survey2D): geometry and picks resident on the GPU,
+  all sources of an evaluation in one call, device tensors in and out.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import PFAST_MIXED, PFAST_PLAIN_FP64, PfastError, check, lib
+
+__all__ = ["fsm3d", "adjoint_fsm3d", "RT_fsm2d", "Tadjoint_fsm2d", "Radjoint_fsm2d", "Context", "Survey3D",
+           "Survey2D", "eval3d_host", "forward3d_host", "PfastError", "PFAST_PLAIN_FP64", "PFAST_MIXED"]
+
+
+def _arr(a, dtype, name, writable=False):
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+        raise TypeError(f"{name}: expected a C-contiguous {np.dtype(dtype).name} numpy array")
+    if writable and not a.flags.writeable:
+        raise TypeError(f"{name}: array is read-only")
+    return a.ctypes.data
+
+
+# ------------------------------------------------------------ reference-signature layer
+def fsm3d(vp, U, src, srcid, MAXSwp, dx, dy, dz, nrows, ncols, nz, pe=0):
+    """First-arrival traveltime of source `srcid` into U (in place)."""
+    n = nrows * ncols * nz
+    if vp.size < n or U.size < n:
+        raise ValueError("vp / U smaller than nrows*ncols*nz")
+    check(lib().pfast_fsm3d(_arr(vp, np.float64, "vp"), _arr(U, np.float64, "U", True), _arr(src, np.int32, "src"),
+                            srcid, MAXSwp, dx, dy, dz, nrows, ncols, nz, pe), "fsm3d")
+
+
+def adjoint_fsm3d(U, T, T_obs, rec, nxyz, src, srnum, srcid, MAXSwp, dx, dy, dz, nrows, ncols, nz, pe=0):
+    """Adjoint state of source `srcid` into U (in place); returns the misfit EE."""
+    EE = C.c_double(0.0)
+    check(lib().pfast_adjoint_fsm3d(_arr(U, np.float64, "U", True), _arr(T, np.float64, "T"),
+                                    _arr(T_obs, np.float64, "T_obs"), _arr(rec, np.int32, "rec"),
+                                    _arr(nxyz, np.float64, "nxyz"), _arr(src, np.int32, "src"),
+                                    _arr(srnum, np.int32, "srnum"), srcid, MAXSwp, dx, dy, dz, nrows, ncols, nz, pe,
+                                    C.addressof(EE)), "adjoint_fsm3d")
+    return EE.value
+
+
+def RT_fsm2d(vp, U, TTd, TTu, Z, src, rec, srnum, srcid, NumofR, MAXSwp, dx, dz, nrows, ncols, pe=0):
+    """Transmission field into U and down/up-going reflection fields into TTd/TTu."""
+    z = np.zeros(1, np.float64)
+    zi = np.zeros(1, np.int32)
+    check(lib().pfast_RT_fsm2d(_arr(vp, np.float64, "vp"), _arr(U, np.float64, "U", True),
+                               _arr(TTd if NumofR else z, np.float64, "TTd", True),
+                               _arr(TTu if NumofR else z, np.float64, "TTu", True),
+                               _arr(Z if NumofR else z, np.float64, "Z"), _arr(src, np.int32, "src"),
+                               _arr(rec if rec is not None else zi, np.int32, "rec"),
+                               _arr(srnum if srnum is not None else zi, np.int32, "srnum"), srcid, NumofR, MAXSwp,
+                               dx, dz, nrows, ncols, pe), "RT_fsm2d")
+
+
+def Tadjoint_fsm2d(U, T, T_obs, rec, nxyz, src, srnum, srcid, MAXSwp, dx, dz, nrows, ncols, pe=0):
+    EE = C.c_double(0.0)
+    check(lib().pfast_Tadjoint_fsm2d(_arr(U, np.float64, "U", True), _arr(T, np.float64, "T"),
+                                     _arr(T_obs, np.float64, "T_obs"), _arr(rec, np.int32, "rec"),
+                                     _arr(nxyz, np.float64, "nxyz"), _arr(src, np.int32, "src"),
+                                     _arr(srnum, np.int32, "srnum"), srcid, MAXSwp, dx, dz, nrows, ncols, pe,
+                                     C.addressof(EE)), "Tadjoint_fsm2d")
+    return EE.value
+
+
+def Radjoint_fsm2d(UR, Td, Tu, TR_obs, rec, nxyz, src, srnum, srcid, NumofR, MAXSwp, dx, dz, nrows, ncols, pe=0):
+    EE = C.c_double(0.0)
+    check(lib().pfast_Radjoint_fsm2d(_arr(UR, np.float64, "UR", True), _arr(Td, np.float64, "Td"),
+                                     _arr(Tu, np.float64, "Tu"), _arr(TR_obs, np.float64, "TR_obs"),
+                                     _arr(rec, np.int32, "rec"), _arr(nxyz, np.float64, "nxyz"),
+                                     _arr(src, np.int32, "src"), _arr(srnum, np.int32, "srnum"), srcid, NumofR,
+                                     MAXSwp, dx, dz, nrows, ncols, pe, C.addressof(EE)), "Radjoint_fsm2d")
+    return EE.value
+
+
+# ------------------------------------------------------------ batched layer
+def _opts(precision, maxswp, max_batch):
+    o = _capi.Options()
+    o.precision = int(precision)
+    o.maxswp = int(maxswp)
+    o.max_batch = int(max_batch)
+    return o
+
+
+class Context:
+    """A device context: one CUDA stream and the reusable device work buffers."""
+
+    def __init__(self, device=0):
+        self._h = C.c_void_p()
+        check(lib().pfast_ctx_create(device, C.byref(self._h)), "ctx_create")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle):
+        """Run on a cudaStream_t (an int handle, e.g. torch.cuda.current_stream().cuda_stream); None = own stream."""
+        check(lib().pfast_ctx_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None), "set_stream")
+
+    def synchronize(self):
+        check(lib().pfast_ctx_synchronize(self._h), "synchronize")
+
+    def close(self):
+        if self._h:
+            lib().pfast_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _dev_ptr(t, name, dtype_name="float64", numel=None):
+    if not getattr(t, "is_cuda", False):
+        raise TypeError(f"{name}: expected a CUDA tensor")
+    if str(t.dtype) != f"torch.{dtype_name}" or not t.is_contiguous():
+        raise TypeError(f"{name}: expected a contiguous {dtype_name} CUDA tensor")
+    if numel is not None and t.numel() < numel:
+        raise ValueError(f"{name}: needs {numel} elements, has {t.numel()}")
+    return t.data_ptr()
+
+
+class Survey3D:
+    """3D acquisition geometry + picks resident on the device.
+
+    src: int32 [nsrc, 3] (row, col, z) node indices; srnum: int32 [nsrc];
+    rec: int32 [sum(srnum), 3]; nxyz: float64 [sum(srnum), 3] (n_y, n_x, n_z);
+    tobs: float64 [sum(srnum)] (rows with tobs >= 100 are not picked).
+    """
+
+    def __init__(self, ctx, nrows, ncols, nz, dx, dy, dz, src, srnum, rec, nxyz=None, tobs=None):
+        self.ctx = ctx
+        self.shape = (nz, nrows, ncols)
+        self.nsrc = len(srnum)
+        self.nrec = int(np.asarray(srnum).sum())
+        src = np.ascontiguousarray(src, np.int32)
+        srnum = np.ascontiguousarray(srnum, np.int32)
+        rec = np.ascontiguousarray(rec, np.int32)
+        self._keep = [src, srnum, rec]
+        nx = tx = None
+        if nxyz is not None:
+            nx = np.ascontiguousarray(nxyz, np.float64)
+            tx = np.ascontiguousarray(tobs, np.float64)
+            self._keep += [nx, tx]
+        self._h = C.c_void_p()
+        check(lib().pfast_survey3d_create(ctx.handle, nrows, ncols, nz, dx, dy, dz, self.nsrc, src.ctypes.data,
+                                          srnum.ctypes.data, rec.ctypes.data, nx.ctypes.data if nx is not None else None,
+                                          tx.ctypes.data if tx is not None else None, C.byref(self._h)),
+              "survey3d_create")
+
+    def eval(self, vp, grad=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0):
+        """Misfit + gradient for the device model vp (torch float64 [nz, nrows, ncols]).
+        Returns (grad tensor, misfit, stats dict)."""
+        import torch
+        n = int(np.prod(self.shape))
+        if grad is None:
+            grad = torch.empty(self.shape, dtype=torch.float64, device=vp.device)
+        E = C.c_double(0)
+        st = _capi.Stats()
+        o = _opts(precision, maxswp, max_batch)
+        check(lib().pfast_survey3d_eval(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
+                                        _dev_ptr(grad, "grad", numel=n), C.addressof(E), C.byref(st)), "survey3d_eval")
+        return grad, E.value, st.as_dict()
+
+    def forward(self, vp, picks=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0):
+        """First-arrival picks [sum(srnum)] for the device model vp.  Returns (picks, stats)."""
+        import torch
+        n = int(np.prod(self.shape))
+        if picks is None:
+            picks = torch.empty(max(self.nrec, 1), dtype=torch.float64, device=vp.device)
+        st = _capi.Stats()
+        o = _opts(precision, maxswp, max_batch)
+        check(lib().pfast_survey3d_forward(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
+                                           _dev_ptr(picks, "picks", numel=self.nrec), C.byref(st)), "survey3d_forward")
+        return picks[:self.nrec], st.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().pfast_survey3d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Survey2D:
+    """2D geometry, picks and reflectors resident on the device.
+
+    src: int32 [nsrc, 2] (row, col); rec: int32 [nrec, 2]; nxy: float64 [nrec, 2] (n_z, n_x);
+    tt_obs: float64 [nrec]; tr_obs: float64 [nrec, numofr]; Z: float64 [numofr*ncols, 3].
+    """
+
+    def __init__(self, ctx, nrows, ncols, dx, dz, src, srnum, rec, numofr=0, Z=None, nxy=None, tt_obs=None,
+                 tr_obs=None):
+        self.ctx = ctx
+        self.shape = (nrows, ncols)
+        self.numofr = numofr
+        self.nsrc = len(srnum)
+        src = np.ascontiguousarray(src, np.int32)
+        srnum = np.ascontiguousarray(srnum, np.int32)
+        rec = np.ascontiguousarray(rec, np.int32)
+        self.nrec = int(rec.shape[0])
+        arrs = [src, srnum, rec]
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        Zc = np.ascontiguousarray(Z, np.float64) if (Z is not None and numofr) else None
+        nx = np.ascontiguousarray(nxy, np.float64) if nxy is not None else None
+        tt = np.ascontiguousarray(tt_obs, np.float64) if tt_obs is not None else None
+        tr = np.ascontiguousarray(tr_obs, np.float64) if (tr_obs is not None and numofr) else None
+        self._keep = arrs + [Zc, nx, tt, tr]
+        self._h = C.c_void_p()
+        check(lib().pfast_survey2d_create(ctx.handle, nrows, ncols, dx, dz, self.nsrc, ptr(src), ptr(srnum),
+                                          self.nrec, ptr(rec), ptr(nx), ptr(tt), numofr, ptr(tr), ptr(Zc),
+                                          C.byref(self._h)), "survey2d_create")
+
+    def forward(self, vp, precision=PFAST_PLAIN_FP64, maxswp=500, max_batch=0):
+        """Picks Tr [nrec, numofr+1] (transmission, then each reflector).  Returns (Tr, stats)."""
+        import torch
+        n = self.shape[0] * self.shape[1]
+        Tr = torch.zeros((max(self.nrec, 1), self.numofr + 1), dtype=torch.float64, device=vp.device)
+        st = _capi.Stats()
+        o = _opts(precision, maxswp, max_batch)
+        check(lib().pfast_survey2d_forward(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
+                                           Tr.data_ptr(), C.byref(st)), "survey2d_forward")
+        return Tr[:self.nrec], st.as_dict()
+
+    def eval(self, vp, WR, precision=PFAST_PLAIN_FP64, maxswp=500, max_batch=0):
+        """Joint gradient.  Returns dict(gT, gR, gRT, Et, Er, stats)."""
+        import torch
+        n = self.shape[0] * self.shape[1]
+        gT, gR, gRT = (torch.empty(self.shape, dtype=torch.float64, device=vp.device) for _ in range(3))
+        Et, Er = C.c_double(0), C.c_double(0)
+        st = _capi.Stats()
+        o = _opts(precision, maxswp, max_batch)
+        check(lib().pfast_survey2d_eval(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n),
+                                        _dev_ptr(WR, "WR", numel=n), C.byref(o), gT.data_ptr(), gR.data_ptr(),
+                                        gRT.data_ptr(), C.addressof(Et), C.addressof(Er), C.byref(st)),
+              "survey2d_eval")
+        return dict(gT=gT, gR=gR, gRT=gRT, Et=Et.value, Er=Er.value, stats=st.as_dict())
+
+    def close(self):
+        if self._h:
+            lib().pfast_survey2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def eval3d_host(ctx, vp, dx, dy, dz, src, srnum, rec, nxyz, tobs, precision=PFAST_PLAIN_FP64, maxswp=100,
+                max_batch=0, grad=None):
+    """One-call host-buffer evaluation (pfast_eval3d): copies in, evaluates, copies the gradient out.
+    vp: float64 [nz, nrows, ncols] host array.  Returns (grad, misfit, stats)."""
+    nz, nr, nc = vp.shape
+    if grad is None:
+        grad = np.empty_like(vp)
+    src = np.ascontiguousarray(src, np.int32)
+    srnum = np.ascontiguousarray(srnum, np.int32)
+    rec = np.ascontiguousarray(rec, np.int32)
+    nxyz = np.ascontiguousarray(nxyz, np.float64)
+    tobs = np.ascontiguousarray(tobs, np.float64)
+    E = C.c_double(0)
+    st = _capi.Stats()
+    o = _opts(precision, maxswp, max_batch)
+    check(lib().pfast_eval3d(ctx.handle, _arr(vp, np.float64, "vp"), nr, nc, nz, dx, dy, dz, len(srnum),
+                             src.ctypes.data, srnum.ctypes.data, rec.ctypes.data, nxyz.ctypes.data, tobs.ctypes.data,
+                             C.byref(o), _arr(grad, np.float64, "grad", True), C.addressof(E), C.byref(st)), "eval3d")
+    return grad, E.value, st.as_dict()
+
+
+def forward3d_host(ctx, vp, dx, dy, dz, src, srnum, rec, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0):
+    nz, nr, nc = vp.shape
+    src = np.ascontiguousarray(src, np.int32)
+    srnum = np.ascontiguousarray(srnum, np.int32)
+    rec = np.ascontiguousarray(rec, np.int32)
+    picks = np.empty(max(int(srnum.sum()), 1))
+    st = _capi.Stats()
+    o = _opts(precision, maxswp, max_batch)
+    check(lib().pfast_forward3d(ctx.handle, _arr(vp, np.float64, "vp"), nr, nc, nz, dx, dy, dz, len(srnum),
+                                src.ctypes.data, srnum.ctypes.data, rec.ctypes.data, C.byref(o), picks.ctypes.data,
+                                C.byref(st)), "forward3d")
+    return picks[:int(srnum.sum())], st.as_dict()

@@ -1,0 +1,73 @@
+// common.cuh -- shared definitions of the pfast_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+
+#include "../../include/pfast_gb300.h"
+
+namespace pfast {
+
+// The reference's "infinity" for unreached nodes (INF macro, src/T_pfsm3d.h:12-14).
+constexpr double kInf = 9999999.0;
+// isconv tolerance (src/T_pfsm3d.h:126, src/RT_pfsm2d.h:112).
+constexpr double kConvTol = 1e-9;
+
+// ---------------------------------------------------------------- 3D tiles
+// One warp sweeps one TK x TI x TJ tile.  Lane = (lk, li), TK*TI == 32; each lane
+// walks its own j-pencil, starting one step after its upstream lanes, so the lanes
+// of a step form one anti-diagonal hyperplane lk+li+lj = t of the tile.
+constexpr int TK = 4, TI = 8, TJ = 32;
+static_assert(TK * TI == 32, "one lane per (k,i) pencil");
+// Halo box in shared memory: (TK+2) planes x (TI+2) rows x (TJ+2) columns.  The plane
+// stride PS is padded so that the 32 lanes of a diagonal step hit distinct banks
+// (address = lk*(PS-1) + li*(HJ-1) + t with HJ-1 = 33 = 1 mod 32 and PS-1 = 8 mod 32).
+constexpr int HK = TK + 2, HI = TI + 2, HJ = TJ + 2, PS = 361;
+static_assert(PS >= HI * HJ && (PS - 1) % 32 == 8 && (HJ - 1) % 32 == 1, "bank-conflict-free stride");
+// Interior tile (slowness) layout: [TK][SPS] with rows of SJ.
+constexpr int SJ = TJ + 2, SPS = 297;
+static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
+// Warps (tiles) per CTA.
+constexpr int kWarps3 = 4;
+
+// ---------------------------------------------------------------- 2D tiles
+// One warp sweeps one T2I x T2J tile; lane = row, pencil along j.
+constexpr int T2I = 32, T2J = 64;
+constexpr int H2I = T2I + 2, H2J = T2J + 2;
+// Row stride: lane li at step t touches li*(R2-1) + t; R2-1 = 65 = 1 mod 32 puts the
+// 32 lanes of a step on 32 distinct banks.
+constexpr int R2 = 66 + 0;
+static_assert(R2 >= H2J && (R2 - 1) % 32 == 1, "bank-conflict-free row stride");
+constexpr int kWarps2 = 4;
+
+// Spacing constants, axis 0 = x (columns j, dx), 1 = y (rows i, dy), 2 = z (k, dz).
+// inv2[a] = (1.0/d)/d exactly as the reference forms 1.0/da/da (src/T_pfsm3d.h:115).
+struct Spacing3 {
+    double d[3];
+    double d2[3];    // d*d
+    double inv2[3];  // (1.0/d)/d
+};
+
+// Which kernel flavour a sweep runs.
+enum SweepKind : int {
+    kFwdPlain64 = 0,   // reference arithmetic, FP64, U = min(U, q)
+    kFwdFast32 = 1,    // FP32 bulk sweeps
+    kFwdPolish64 = 2,  // FP64 polish from a near-converged field
+    kAdjPlain64 = 3,   // reference arithmetic, FP64
+    kAdjFast32 = 4,    // FP32 bulk adjoint sweeps
+    kAdjPolish64 = 5,  // FP64 adjoint polish
+};
+
+}  // namespace pfast
+
+#define PFAST_CUDA_TRY(expr)                                                        \
+    do {                                                                            \
+        cudaError_t e__ = (expr);                                                   \
+        if (e__ != cudaSuccess) return ::pfast::cuda_fail(e__, #expr, __FILE__, __LINE__); \
+    } while (0)
+
+namespace pfast {
+pfast_status cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+void set_last_error(const char* fmt, ...);
+}  // namespace pfast

@@ -1,0 +1,771 @@
+// engine.cu -- runtime of pfast_gb300: context, device buffers, 3D surveys, the
+// outer-iteration driver, the 3D pipelines and the C ABI.
+//
+// The per-source loops of the reference drivers (src/T_PFAST3D.cpp:387-399,
+// 672-686) become batches of sources on one GPU.  Every solve keeps the
+// reference's outer-iteration semantics: an iteration = snapshot + 2^d ordered
+// sweeps, repeated while some node moved by more than 1e-9 and fewer than MAXSwp
+// iterations ran (src/T_pfsm3d.h:152, src/T_padjoint3d.h:135).  Converged sources
+// retire from the batch; the others keep sweeping.
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <unordered_set>
+#include <algorithm>
+
+#include "engine.h"
+
+namespace pfast {
+
+// ------------------------------------------------------------------ errors
+static thread_local char g_err[512] = "";
+
+void set_last_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+pfast_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    set_last_error("%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    return e == cudaErrorMemoryAllocation ? PFAST_ERR_NOMEM : PFAST_ERR_CUDA;
+}
+
+#define PFAST_TRY(expr)                          \
+    do {                                         \
+        pfast_status s__ = (expr);               \
+        if (s__ != PFAST_OK) return s__;         \
+    } while (0)
+
+// ------------------------------------------------------------------ buffers
+pfast_status DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return PFAST_OK;
+    if (p) cudaDeviceSynchronize();   // queued kernels may still use the old allocation
+    release();
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cap = 0;
+        cudaGetLastError();
+        set_last_error("cudaMalloc(%zu bytes) failed: %s", want, cudaGetErrorString(e));
+        return PFAST_ERR_NOMEM;
+    }
+    cap = want;
+    return PFAST_OK;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+
+pfast_status HostBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return PFAST_OK;
+    if (p) cudaDeviceSynchronize();   // an async copy may still read or write the old buffer
+    release();
+    size_t want = std::max<size_t>(bytes, 4096);
+    PFAST_CUDA_TRY(cudaMallocHost(&p, want));
+    cap = want;
+    return PFAST_OK;
+}
+
+void HostBuf::release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+}
+
+void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && acc) *acc += ms;
+}
+
+pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, DiagTable3** out) {
+    auto key = std::make_tuple(nz, nr, nc);
+    auto it = ctx->diag3.find(key);
+    if (it == ctx->diag3.end()) {
+        DiagTable3 t;
+        PFAST_TRY(build_diag_table3(nz, nr, nc, t));
+        it = ctx->diag3.emplace(key, t).first;
+    }
+    *out = &it->second;
+    return PFAST_OK;
+}
+
+pfast_status ctx_diag2(pfast_ctx* ctx, int nr, int nc, DiagTable2** out) {
+    auto key = std::make_pair(nr, nc);
+    auto it = ctx->diag2.find(key);
+    if (it == ctx->diag2.end()) {
+        DiagTable2 t;
+        PFAST_TRY(build_diag_table2(nr, nc, t));
+        it = ctx->diag2.emplace(key, t).first;
+    }
+    *out = &it->second;
+    return PFAST_OK;
+}
+
+// ------------------------------------------------------------------ sweep driver
+namespace {
+
+// FP32 bulk phases stop once no node moves by more than ~8 ulps (relative);
+// FP64 phases use the reference's absolute 1e-9.
+constexpr double kTol32Rel = 1.0 / (1 << 20);
+constexpr double kTol32AbsAdj = 1e-6;
+
+Spacing3 make_spacing(double dx, double dy, double dz) {
+    Spacing3 s;
+    const double d[3] = {dx, dy, dz};
+    for (int a = 0; a < 3; ++a) {
+        s.d[a] = d[a];
+        s.d2[a] = d[a] * d[a];
+        s.inv2[a] = 1.0 / d[a] / d[a];
+    }
+    return s;
+}
+
+// Run outer iterations of `kind` over the active batch instances until each one
+// converges or reaches maxiter.  iters[b] receives the iteration count of instance b.
+pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable3& dt, int nb,
+                         std::vector<int>& active, int maxiter, int* iters, long long nodes_per_sweep,
+                         long long* node_updates, int* not_conv, double* ms_acc) {
+    PFAST_TRY(ctx->act.ensure(sizeof(int) * nb));
+    PFAST_TRY(ctx->changed.ensure(sizeof(int) * nb));
+    PFAST_TRY(ctx->h_act.ensure(sizeof(int) * nb));
+    PFAST_TRY(ctx->h_changed.ensure(sizeof(int) * nb));
+    int* h_act = ctx->h_act.as<int>();
+    int* h_chg = ctx->h_changed.as<int>();
+    a.act = ctx->act.as<int>();
+    a.changed = ctx->changed.as<int>();
+    a.diag_off = dt.d_off;
+    a.diag_tiles = dt.d_tiles;
+    a.nbk = dt.nbk;
+    a.nbi = dt.nbi;
+    a.nbj = dt.nbj;
+    cudaStream_t st = ctx->stream;
+    PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
+    int it = 0;
+    while (!active.empty() && it < maxiter) {
+        const int nact = (int)active.size();
+        std::memcpy(h_act, active.data(), sizeof(int) * nact);
+        PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
+        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));
+        for (int dir = 0; dir < 8; ++dir) {
+            a.dir = dir;
+            a.first = dir == 0;
+            a.last = dir == 7;
+            for (int d = 0; d < dt.ndiag; ++d) {
+                PFAST_TRY(launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
+                ++ctx->launches;
+            }
+        }
+        cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) return cuda_fail(le, "sweep launch", __FILE__, __LINE__);
+        PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+        PFAST_CUDA_TRY(cudaStreamSynchronize(st));
+        ++it;
+        if (node_updates) *node_updates += (long long)nact * 8 * nodes_per_sweep;
+        std::vector<int> still;
+        still.reserve(nact);
+        for (int id : active) {
+            iters[id] = it;
+            if (h_chg[id]) still.push_back(id);
+        }
+        active.swap(still);
+    }
+    if (not_conv) *not_conv += (int)active.size();
+    PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[1], st));
+    add_elapsed(ctx->ev[0], ctx->ev[1], ms_acc);
+    return PFAST_OK;
+}
+
+Sweep3Args base_args(const pfast_survey3d* sv) {
+    Sweep3Args a;
+    std::memset(&a, 0, sizeof(a));
+    a.nz = sv->nz;
+    a.nr = sv->nr;
+    a.nc = sv->nc;
+    a.sp = make_spacing(sv->dx, sv->dy, sv->dz);
+    a.wpr = (sv->nc + 31) / 32;
+    return a;
+}
+
+}  // namespace
+
+pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, int nb, int precision, int maxswp,
+                             pfast_stats* st) {
+    const long long N = (long long)sv->nz * sv->nr * sv->nc;
+    cudaStream_t s = ctx->stream;
+    DiagTable3* dt = nullptr;
+    PFAST_TRY(ctx_diag3(ctx, sv->nz, sv->nr, sv->nc, &dt));
+    PFAST_TRY(ctx->T64.ensure(sizeof(double) * N * nb));
+    PFAST_TRY(ctx->scratch.ensure(sizeof(double) * N * nb));
+    std::vector<int> iters(nb, 0), active(nb);
+    Sweep3Args a = base_args(sv);
+    a.fstride = N;
+    a.src_kij = sv->d_src_kij + 3 * b0;
+    const long long* src_lin = sv->d_src_lin + b0;
+    int dummy_nc = 0;
+    int* nc_ptr = st ? &st->not_converged : &dummy_nc;
+    long long* nu = st ? &st->fwd_node_updates : nullptr;
+    if (precision == PFAST_PLAIN_FP64) {
+        PFAST_TRY(launch_init_fwd3(ctx->T64.p, 0, N, N, src_lin, nb, s));
+        for (int b = 0; b < nb; ++b) active[b] = b;
+        a.field = ctx->T64.p;
+        a.snap = ctx->scratch.p;
+        a.aux = ctx->s64.p;
+        a.tol_abs = kConvTol;
+        a.tol_rel = 0.0;
+        long long before = nu ? *nu : 0;
+        PFAST_TRY(run_sweeps3(ctx, a, kFwdPlain64, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
+                              st ? &st->ms_fwd64 : nullptr));
+        if (st) {
+            st->fwd64_node_updates += *nu - before;
+            for (int v : iters) st->fwd_iters_max = std::max(st->fwd_iters_max, v);
+        }
+    } else {
+        float* T32 = ctx->scratch.as<float>();
+        float* snap32 = T32 + N * nb;
+        PFAST_TRY(launch_init_fwd3(T32, 1, N, N, src_lin, nb, s));
+        for (int b = 0; b < nb; ++b) active[b] = b;
+        a.field = T32;
+        a.snap = snap32;
+        a.aux = ctx->s32.p;
+        a.tol_abs = 0.0;
+        a.tol_rel = kTol32Rel;
+        PFAST_TRY(run_sweeps3(ctx, a, kFwdFast32, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
+                              st ? &st->ms_fwd32 : nullptr));
+        if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
+        PFAST_TRY(launch_widen(T32, ctx->T64.as<double>(), N, N, N, nb, s));
+        std::fill(iters.begin(), iters.end(), 0);
+        active.resize(nb);
+        for (int b = 0; b < nb; ++b) active[b] = b;
+        a.field = ctx->T64.p;
+        a.snap = ctx->scratch.p;
+        a.aux = ctx->s64.p;
+        a.tol_abs = kConvTol;
+        a.tol_rel = 0.0;
+        long long before = nu ? *nu : 0;
+        PFAST_TRY(run_sweeps3(ctx, a, kFwdPolish64, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
+                              st ? &st->ms_fwd64 : nullptr));
+        if (st) {
+            st->fwd64_node_updates += *nu - before;
+            for (int v : iters) st->fwd_iters_max = std::max(st->fwd_iters_max, v);
+        }
+    }
+    return PFAST_OK;
+}
+
+pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, int nb, int precision, int maxswp,
+                             double* ee_out, pfast_stats* st) {
+    const long long N = (long long)sv->nz * sv->nr * sv->nc;
+    const int wpr = (sv->nc + 31) / 32;
+    const long long mwords = (long long)sv->nz * sv->nr * wpr;
+    cudaStream_t s = ctx->stream;
+    DiagTable3* dt = nullptr;
+    PFAST_TRY(ctx_diag3(ctx, sv->nz, sv->nr, sv->nc, &dt));
+    PFAST_TRY(ctx->L64.ensure(sizeof(double) * N * nb));
+    PFAST_TRY(ctx->scratch.ensure(sizeof(double) * N * nb));
+    PFAST_TRY(ctx->mask.ensure(sizeof(unsigned) * mwords * nb));
+    PFAST_TRY(ctx->ee.ensure(sizeof(double) * nb));
+    PFAST_TRY(ctx->need.ensure(sizeof(int) * nb));
+    PFAST_TRY(ctx->h_ee.ensure(sizeof(double) * nb));
+    PFAST_TRY(ctx->h_need.ensure(sizeof(int) * nb));
+    PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+    PFAST_CUDA_TRY(cudaMemsetAsync(ctx->L64.p, 0, sizeof(double) * N * nb, s));
+    PFAST_CUDA_TRY(cudaMemsetAsync(ctx->mask.p, 0, sizeof(unsigned) * mwords * nb, s));
+    Bc3Args bc;
+    bc.T = ctx->T64.as<double>();
+    bc.L = ctx->L64.as<double>();
+    bc.fstride = N;
+    bc.mask = ctx->mask.as<unsigned>();
+    bc.mask_stride = mwords;
+    bc.wpr = wpr;
+    bc.rec = sv->d_rec;
+    bc.nxyz = sv->d_nxyz;
+    bc.tobs = sv->d_tobs;
+    bc.last = sv->d_last;
+    bc.ch0 = sv->d_ch0 + b0;
+    bc.srnum = sv->d_srnum + b0;
+    bc.src_kij = sv->d_src_kij + 3 * b0;
+    bc.EE = ctx->ee.as<double>();
+    bc.need = ctx->need.as<int>();
+    bc.nz = sv->nz;
+    bc.nr = sv->nr;
+    bc.nc = sv->nc;
+    bc.dx = sv->dx;
+    bc.dy = sv->dy;
+    bc.dz = sv->dz;
+    PFAST_TRY(launch_bc3(bc, nb, s));
+    PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->h_ee.p, ctx->ee.p, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
+    PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->h_need.p, ctx->need.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, s));
+    PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
+    PFAST_CUDA_TRY(cudaStreamSynchronize(s));
+    add_elapsed(ctx->ev[2], ctx->ev[3], st ? &st->ms_other : nullptr);
+    std::memcpy(ee_out, ctx->h_ee.p, sizeof(double) * nb);
+    std::vector<int> active, iters(nb, 0);
+    for (int b = 0; b < nb; ++b)
+        if (ctx->h_need.as<int>()[b]) active.push_back(b);
+    const long long interior =
+        (long long)std::max(0, sv->nz - 2) * std::max(0, sv->nr - 2) * std::max(0, sv->nc - 2);
+    Sweep3Args a = base_args(sv);
+    a.fstride = N;
+    a.mask = ctx->mask.as<unsigned>();
+    a.mask_stride = mwords;
+    a.aux = ctx->T64.p;
+    int dummy_nc = 0;
+    int* nc_ptr = st ? &st->not_converged : &dummy_nc;
+    long long* nu = st ? &st->adj_node_updates : nullptr;
+    if (precision == PFAST_PLAIN_FP64) {
+        a.field = ctx->L64.p;
+        a.snap = ctx->scratch.p;
+        a.tol_abs = kConvTol;
+        a.tol_rel = 0.0;
+        long long before = nu ? *nu : 0;
+        PFAST_TRY(run_sweeps3(ctx, a, kAdjPlain64, *dt, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
+                              st ? &st->ms_adj64 : nullptr));
+        if (st) {
+            st->adj64_node_updates += *nu - before;
+            for (int v : iters) st->adj_iters_max = std::max(st->adj_iters_max, v);
+        }
+    } else {
+        std::vector<int> active64 = active;
+        float* L32 = ctx->scratch.as<float>();
+        float* snap32 = L32 + N * nb;
+        PFAST_TRY(launch_narrow(ctx->L64.as<double>(), L32, N, N, N, nb, s));
+        a.field = L32;
+        a.snap = snap32;
+        a.tol_abs = kTol32AbsAdj;
+        a.tol_rel = kTol32Rel;
+        PFAST_TRY(run_sweeps3(ctx, a, kAdjFast32, *dt, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
+                              st ? &st->ms_adj32 : nullptr));
+        if (st) for (int v : iters) st->adj32_iters_max = std::max(st->adj32_iters_max, v);
+        PFAST_TRY(launch_widen_lambda(L32, ctx->L64.as<double>(), ctx->mask.as<unsigned>(), N, N, mwords, sv->nz,
+                                      sv->nr, sv->nc, wpr, nb, s));
+        std::fill(iters.begin(), iters.end(), 0);
+        a.field = ctx->L64.p;
+        a.snap = ctx->scratch.p;
+        a.tol_abs = kConvTol;
+        a.tol_rel = 0.0;
+        long long before = nu ? *nu : 0;
+        PFAST_TRY(run_sweeps3(ctx, a, kAdjPolish64, *dt, nb, active64, maxswp, iters.data(), interior, nu, nc_ptr,
+                              st ? &st->ms_adj64 : nullptr));
+        if (st) {
+            st->adj64_node_updates += *nu - before;
+            for (int v : iters) st->adj_iters_max = std::max(st->adj_iters_max, v);
+        }
+    }
+    return PFAST_OK;
+}
+
+namespace {
+
+bool valid_options(const pfast_options* opt) {
+    if (!opt) return true;
+    if (opt->precision != PFAST_PLAIN_FP64 && opt->precision != PFAST_MIXED) {
+        set_last_error("unknown precision %d", opt->precision);
+        return false;
+    }
+    if (opt->maxswp < 0 || opt->max_batch < 0) {
+        set_last_error("negative maxswp / max_batch");
+        return false;
+    }
+    return true;
+}
+
+pfast_options resolve(const pfast_options* opt, int default_maxswp) {
+    pfast_options o;
+    o.precision = PFAST_PLAIN_FP64;
+    o.maxswp = default_maxswp;
+    o.max_batch = 0;
+    if (opt) o = *opt;
+    return o;
+}
+
+// Sources per batch: the caller's cap, else what fits in 85% of free device memory.
+int pick_batch(int nsrc, int max_batch, size_t bytes_per_src) {
+    int b = nsrc;
+    if (max_batch > 0) b = std::min(b, max_batch);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes_per_src > 0) {
+        size_t fit = (size_t)(0.85 * (double)fr) / bytes_per_src;
+        b = (int)std::min<size_t>((size_t)b, std::max<size_t>(1, fit));
+    }
+    return std::max(1, std::min(b, 65535));
+}
+
+void stats_begin(pfast_stats* st) {
+    if (st) std::memset(st, 0, sizeof(*st));
+}
+
+}  // namespace
+
+}  // namespace pfast
+
+using namespace pfast;
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* pfast_version(void) { return "pfast_gb300 0.1 (sm_103a)"; }
+
+const char* pfast_status_string(pfast_status s) {
+    switch (s) {
+        case PFAST_OK: return "ok";
+        case PFAST_ERR_INVALID: return "invalid argument";
+        case PFAST_ERR_CUDA: return "CUDA error";
+        case PFAST_ERR_NOMEM: return "out of device memory";
+        case PFAST_ERR_NO_DEVICE: return "no CUDA device";
+        case PFAST_ERR_NO_REFLECTION_POINT: return "no node above a reflector";
+        case PFAST_ERR_NEGATIVE_TIME: return "negative reflected traveltime";
+    }
+    return "unknown status";
+}
+
+const char* pfast_last_error(void) { return g_err; }
+
+void pfast_default_options(pfast_options* opt) {
+    if (!opt) return;
+    opt->precision = PFAST_PLAIN_FP64;
+    opt->maxswp = 100;
+    opt->max_batch = 0;
+}
+
+pfast_status pfast_ctx_create(int device, pfast_ctx** out) {
+    if (!out) { set_last_error("null output pointer"); return PFAST_ERR_INVALID; }
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        set_last_error("no CUDA device visible");
+        return PFAST_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) { set_last_error("device %d out of range (%d devices)", device, n); return PFAST_ERR_INVALID; }
+    PFAST_CUDA_TRY(cudaSetDevice(device));
+    pfast_ctx* c = new pfast_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__); }
+    c->stream = c->own_stream;
+    for (auto& ev : c->ev) {
+        e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__); }
+    }
+    *out = c;
+    return PFAST_OK;
+}
+
+pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
+    if (!ctx) return PFAST_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
+                      &ctx->ee, &ctx->need, &ctx->misc, &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a,
+                      &ctx->f2b, &ctx->f2c})
+        b->release();
+    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need}) b->release();
+    for (auto& kv : ctx->diag3) free_diag_table3(kv.second);
+    for (auto& kv : ctx->diag2) free_diag_table2(kv.second);
+    for (auto& ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return PFAST_OK;
+}
+
+pfast_status pfast_ctx_set_stream(pfast_ctx* ctx, void* stream) {
+    if (!ctx) { set_last_error("null context"); return PFAST_ERR_INVALID; }
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return PFAST_OK;
+}
+
+pfast_status pfast_ctx_synchronize(pfast_ctx* ctx) {
+    if (!ctx) { set_last_error("null context"); return PFAST_ERR_INVALID; }
+    PFAST_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return PFAST_OK;
+}
+
+// ------------------------------------------------------------------ 3D surveys
+pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz, double dx, double dy, double dz,
+                                   int nsrc, const int* src, const int* srnum, const int* rec, const double* nxyz,
+                                   const double* T_obs, pfast_survey3d** out) {
+    if (!ctx || !out) { set_last_error("null context or output"); return PFAST_ERR_INVALID; }
+    *out = nullptr;
+    if (nrows < 2 || ncols < 2 || nz < 2) {
+        set_last_error("3D grid %dx%dx%d: every dimension must be >= 2", nrows, ncols, nz);
+        return PFAST_ERR_INVALID;
+    }
+    if (!(dx > 0 && dy > 0 && dz > 0)) { set_last_error("grid spacings must be positive"); return PFAST_ERR_INVALID; }
+    if (nsrc < 0 || (nsrc > 0 && (!src || !srnum))) { set_last_error("bad source arrays"); return PFAST_ERR_INVALID; }
+    long long nrec = 0;
+    for (int s = 0; s < nsrc; ++s) {
+        if (srnum[s] < 0) { set_last_error("srnum[%d] < 0", s); return PFAST_ERR_INVALID; }
+        nrec += srnum[s];
+        const int i = src[3 * s], j = src[3 * s + 1], k = src[3 * s + 2];
+        if (i < 0 || i >= nrows || j < 0 || j >= ncols || k < 0 || k >= nz) {
+            set_last_error("source %d at (%d,%d,%d) outside the %dx%dx%d grid", s, i, j, k, nrows, ncols, nz);
+            return PFAST_ERR_INVALID;
+        }
+    }
+    if (nrec > 0x7fffffffLL) { set_last_error("too many receiver rows"); return PFAST_ERR_INVALID; }
+    if (nrec > 0 && !rec) { set_last_error("null receiver array"); return PFAST_ERR_INVALID; }
+    for (long long r = 0; r < nrec; ++r) {
+        const int i = rec[3 * r], j = rec[3 * r + 1], k = rec[3 * r + 2];
+        if (i < 0 || i >= nrows || j < 0 || j >= ncols || k < 0 || k >= nz) {
+            set_last_error("receiver row %lld at (%d,%d,%d) outside the grid", r, i, j, k);
+            return PFAST_ERR_INVALID;
+        }
+    }
+    PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
+    pfast_survey3d* sv = new pfast_survey3d();
+    sv->ctx = ctx;
+    sv->nz = nz; sv->nr = nrows; sv->nc = ncols;
+    sv->dx = dx; sv->dy = dy; sv->dz = dz;
+    sv->nsrc = nsrc;
+    sv->nrec = (int)nrec;
+    sv->h_src.assign(src, src + 3 * (size_t)nsrc);
+    sv->h_srnum.assign(srnum, srnum + nsrc);
+    sv->h_ch0.assign(nsrc + 1, 0);
+    for (int s = 0; s < nsrc; ++s) sv->h_ch0[s + 1] = sv->h_ch0[s] + srnum[s];
+    std::vector<int> kij(3 * (size_t)std::max(nsrc, 1));
+    std::vector<long long> lin(std::max(nsrc, 1));
+    for (int s = 0; s < nsrc; ++s) {
+        kij[3 * s] = src[3 * s + 2];
+        kij[3 * s + 1] = src[3 * s];
+        kij[3 * s + 2] = src[3 * s + 1];
+        lin[s] = (long long)src[3 * s + 2] * nrows * ncols + (long long)src[3 * s] * ncols + src[3 * s + 1];
+    }
+    // last picked row at each node, per source (the reference's later rows overwrite earlier ones)
+    sv->has_picks = nxyz && T_obs;
+    std::vector<unsigned char> last(std::max<long long>(nrec, 1), 0);
+    if (sv->has_picks) {
+        for (int s = 0; s < nsrc; ++s) {
+            std::unordered_set<long long> seen;
+            for (int r = sv->h_ch0[s + 1] - 1; r >= sv->h_ch0[s]; --r) {
+                if (!(T_obs[r] < 100)) continue;
+                const long long node = (long long)rec[3 * r + 2] * nrows * ncols + (long long)rec[3 * r] * ncols + rec[3 * r + 1];
+                if (seen.insert(node).second) last[r] = 1;
+            }
+        }
+    }
+    auto up = [&](void** dst, const void* h, size_t bytes) -> pfast_status {
+        PFAST_CUDA_TRY(cudaMalloc(dst, std::max<size_t>(bytes, 16)));
+        if (bytes) PFAST_CUDA_TRY(cudaMemcpy(*dst, h, bytes, cudaMemcpyHostToDevice));
+        return PFAST_OK;
+    };
+    pfast_status stt = PFAST_OK;
+    if (!stt) stt = up((void**)&sv->d_src_kij, kij.data(), sizeof(int) * 3 * nsrc);
+    if (!stt) stt = up((void**)&sv->d_src_lin, lin.data(), sizeof(long long) * nsrc);
+    if (!stt) stt = up((void**)&sv->d_ch0, sv->h_ch0.data(), sizeof(int) * (nsrc + 1));
+    if (!stt) stt = up((void**)&sv->d_srnum, srnum, sizeof(int) * nsrc);
+    if (!stt) stt = up((void**)&sv->d_rec, rec, sizeof(int) * 3 * nrec);
+    if (!stt) stt = up((void**)&sv->d_nxyz, sv->has_picks ? nxyz : nullptr, sv->has_picks ? sizeof(double) * 3 * nrec : 0);
+    if (!stt) stt = up((void**)&sv->d_tobs, sv->has_picks ? T_obs : nullptr, sv->has_picks ? sizeof(double) * nrec : 0);
+    if (!stt) stt = up((void**)&sv->d_last, last.data(), sizeof(unsigned char) * nrec);
+    if (stt) { pfast_survey3d_destroy(sv); return stt; }
+    *out = sv;
+    return PFAST_OK;
+}
+
+pfast_status pfast_survey3d_destroy(pfast_survey3d* sv) {
+    if (!sv) return PFAST_OK;
+    for (void* p : {(void*)sv->d_src_kij, (void*)sv->d_src_lin, (void*)sv->d_ch0, (void*)sv->d_srnum, (void*)sv->d_rec,
+                    (void*)sv->d_nxyz, (void*)sv->d_tobs, (void*)sv->d_last})
+        if (p) cudaFree(p);
+    delete sv;
+    return PFAST_OK;
+}
+
+static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
+                                 double* grad, double* misfit, double* picks, pfast_stats* stats) {
+    if (!ctx || !sv || !vp) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
+    if (!valid_options(opt)) return PFAST_ERR_INVALID;
+    const bool want_grad = grad != nullptr;
+    if (want_grad && !sv->has_picks) { set_last_error("survey has no picks: gradient unavailable"); return PFAST_ERR_INVALID; }
+    pfast_options o = resolve(opt, 100);
+    stats_begin(stats);
+    PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
+    const long long N = (long long)sv->nz * sv->nr * sv->nc;
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t t0 = ctx->ev[6], t1 = ctx->ev[7];
+    PFAST_CUDA_TRY(cudaEventRecord(t0, s));
+    const long long launches0 = ctx->launches;
+    PFAST_TRY(ctx->s64.ensure(sizeof(double) * N));
+    PFAST_TRY(ctx->s32.ensure(sizeof(float) * N));
+    PFAST_TRY(launch_slowness(vp, ctx->s64.as<double>(), o.precision == PFAST_MIXED ? ctx->s32.as<float>() : nullptr, N, s));
+    if (want_grad) PFAST_CUDA_TRY(cudaMemsetAsync(grad, 0, sizeof(double) * N, s));
+    const size_t per_src = (size_t)N * (want_grad ? 24 : 16) + (size_t)sv->nz * sv->nr * ((sv->nc + 31) / 32) * 4;
+    const int B = pick_batch(std::max(sv->nsrc, 1), o.max_batch, per_src);
+    double E = 0.0;
+    std::vector<double> ee(B);
+    for (int b0 = 0; b0 < sv->nsrc; b0 += B) {
+        const int nb = std::min(B, sv->nsrc - b0);
+        if (stats) ++stats->batches;
+        PFAST_TRY(forward3d_batch(ctx, sv, b0, nb, o.precision, o.maxswp, stats));
+        if (want_grad) {
+            PFAST_TRY(adjoint3d_batch(ctx, sv, b0, nb, o.precision, o.maxswp, ee.data(), stats));
+            for (int b = 0; b < nb; ++b) E += ee[b];   // loc_E += EE in source order
+            PFAST_TRY(launch_accumulate(grad, ctx->L64.as<double>(), N, vp, N, nb, s));
+        }
+        if (picks) PFAST_TRY(launch_gather3(ctx->T64.as<double>(), N, sv->d_rec, sv->d_ch0 + b0, sv->d_srnum + b0, nb,
+                                            sv->nz, sv->nr, sv->nc, picks, s));
+    }
+    PFAST_CUDA_TRY(cudaEventRecord(t1, s));
+    PFAST_CUDA_TRY(cudaStreamSynchronize(s));
+    if (stats) {
+        add_elapsed(t0, t1, &stats->ms_total);
+        stats->launches = ctx->launches - launches0;
+    }
+    if (misfit) *misfit = E;
+    return PFAST_OK;
+}
+
+pfast_status pfast_survey3d_eval(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
+                                 double* grad, double* misfit, pfast_stats* stats) {
+    if (!grad) { set_last_error("null gradient"); return PFAST_ERR_INVALID; }
+    return survey3d_run(ctx, sv, vp, opt, grad, misfit, nullptr, stats);
+}
+
+pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
+                                    double* picks, pfast_stats* stats) {
+    if (!picks) { set_last_error("null picks"); return PFAST_ERR_INVALID; }
+    return survey3d_run(ctx, sv, vp, opt, nullptr, nullptr, picks, stats);
+}
+
+pfast_status pfast_eval3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy, double dz,
+                          int nsrc, const int* src, const int* srnum, const int* rec, const double* nxyz,
+                          const double* T_obs, const pfast_options* opt, double* grad, double* misfit,
+                          pfast_stats* stats) {
+    if (!ctx || !vp || !grad || !nxyz || !T_obs) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
+    pfast_survey3d* sv = nullptr;
+    PFAST_TRY(pfast_survey3d_create(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nxyz, T_obs, &sv));
+    const long long N = (long long)nrows * ncols * nz;
+    pfast_status r = ctx->vp_tmp.ensure(sizeof(double) * N);
+    if (!r) r = ctx->grad_tmp.ensure(sizeof(double) * N);
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(ctx->vp_tmp.p, vp, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync(vp)", __FILE__, __LINE__);
+    }
+    if (!r) r = survey3d_run(ctx, sv, ctx->vp_tmp.as<double>(), opt, ctx->grad_tmp.as<double>(), misfit, nullptr, stats);
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(grad, ctx->grad_tmp.p, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync(grad)", __FILE__, __LINE__);
+    }
+    pfast_survey3d_destroy(sv);
+    return r;
+}
+
+pfast_status pfast_forward3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy,
+                             double dz, int nsrc, const int* src, const int* srnum, const int* rec,
+                             const pfast_options* opt, double* picks, pfast_stats* stats) {
+    if (!ctx || !vp || !picks) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
+    pfast_survey3d* sv = nullptr;
+    PFAST_TRY(pfast_survey3d_create(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nullptr, nullptr, &sv));
+    const long long N = (long long)nrows * ncols * nz;
+    pfast_status r = ctx->vp_tmp.ensure(sizeof(double) * N);
+    if (!r) r = ctx->picks_tmp.ensure(sizeof(double) * std::max(sv->nrec, 1));
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(ctx->vp_tmp.p, vp, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync(vp)", __FILE__, __LINE__);
+    }
+    if (!r) r = survey3d_run(ctx, sv, ctx->vp_tmp.as<double>(), opt, nullptr, nullptr, ctx->picks_tmp.as<double>(), stats);
+    if (!r && sv->nrec > 0) {
+        cudaError_t e = cudaMemcpyAsync(picks, ctx->picks_tmp.p, sizeof(double) * sv->nrec, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync(picks)", __FILE__, __LINE__);
+    }
+    pfast_survey3d_destroy(sv);
+    return r;
+}
+
+// ------------------------------------------------------------------ reference-signature shims
+static std::mutex g_default_mu;
+static pfast_ctx* g_default[64] = {};
+
+static pfast_status default_ctx(pfast_ctx** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error("no CUDA device");
+        return PFAST_ERR_NO_DEVICE;
+    }
+    if (dev < 0 || dev >= 64) { set_last_error("device id %d unsupported", dev); return PFAST_ERR_INVALID; }
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (!g_default[dev]) PFAST_TRY(pfast_ctx_create(dev, &g_default[dev]));
+    *out = g_default[dev];
+    return PFAST_OK;
+}
+
+}  // extern "C"
+pfast_status pfast::default_context(pfast_ctx** out) { return default_ctx(out); }
+extern "C" {
+
+pfast_status pfast_fsm3d(double* vp, double* U, int* src, int srcid, int MAXSwp, double dx, double dy, double dz,
+                         int nrows, int ncols, int nz, int pe) {
+    (void)pe;
+    if (!vp || !U || !src || srcid < 0) { set_last_error("null argument or negative srcid"); return PFAST_ERR_INVALID; }
+    pfast_ctx* ctx = nullptr;
+    PFAST_TRY(default_ctx(&ctx));
+    int zero = 0;
+    pfast_survey3d* sv = nullptr;
+    PFAST_TRY(pfast_survey3d_create(ctx, nrows, ncols, nz, dx, dy, dz, 1, src + 3 * srcid, &zero, nullptr, nullptr,
+                                    nullptr, &sv));
+    const long long N = (long long)nrows * ncols * nz;
+    pfast_status r = ctx->vp_tmp.ensure(sizeof(double) * N);
+    cudaStream_t s = ctx->stream;
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(ctx->vp_tmp.p, vp, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) r = cuda_fail(e, "copy vp", __FILE__, __LINE__);
+    }
+    if (!r) r = ctx->s64.ensure(sizeof(double) * N);
+    if (!r) r = launch_slowness(ctx->vp_tmp.as<double>(), ctx->s64.as<double>(), nullptr, N, s);
+    if (!r) r = forward3d_batch(ctx, sv, 0, 1, PFAST_PLAIN_FP64, MAXSwp, nullptr);
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(U, ctx->T64.p, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) r = cuda_fail(e, "copy U", __FILE__, __LINE__);
+    }
+    pfast_survey3d_destroy(sv);
+    return r;
+}
+
+pfast_status pfast_adjoint_fsm3d(double* U, double* T, double* T_obs, int* rec, double* nxyz, int* src, int* srnum,
+                                 int srcid, int MAXSwp, double dx, double dy, double dz, int nrows, int ncols, int nz,
+                                 int pe, double* EE) {
+    (void)pe;
+    if (!U || !T || !T_obs || !rec || !nxyz || !src || !srnum || srcid < 0) {
+        set_last_error("null argument or negative srcid");
+        return PFAST_ERR_INVALID;
+    }
+    pfast_ctx* ctx = nullptr;
+    PFAST_TRY(default_ctx(&ctx));
+    long long ch0 = 0;
+    for (int s = 0; s < srcid; ++s) ch0 += srnum[s];
+    pfast_survey3d* sv = nullptr;
+    PFAST_TRY(pfast_survey3d_create(ctx, nrows, ncols, nz, dx, dy, dz, 1, src + 3 * srcid, srnum + srcid,
+                                    rec + 3 * ch0, nxyz + 3 * ch0, T_obs + ch0, &sv));
+    const long long N = (long long)nrows * ncols * nz;
+    cudaStream_t s = ctx->stream;
+    pfast_status r = ctx->T64.ensure(sizeof(double) * N);
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(ctx->T64.p, T, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) r = cuda_fail(e, "copy T", __FILE__, __LINE__);
+    }
+    double ee = 0.0;
+    if (!r) r = adjoint3d_batch(ctx, sv, 0, 1, PFAST_PLAIN_FP64, MAXSwp, &ee, nullptr);
+    if (!r) {
+        cudaError_t e = cudaMemcpyAsync(U, ctx->L64.p, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) r = cuda_fail(e, "copy lambda", __FILE__, __LINE__);
+    }
+    if (!r && EE) *EE = ee;
+    pfast_survey3d_destroy(sv);
+    return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,118 @@
+// engine.h -- host-side runtime of pfast_gb300 (internal): context, device
+// buffers, surveys and the sweep driver.
+#pragma once
+
+#include <map>
+#include <tuple>
+#include <vector>
+#include <string>
+
+#include "kernels.h"
+#include "kernels2d.h"
+
+namespace pfast {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    pfast_status ensure(size_t bytes);
+    void release();
+    template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Pinned host scratch for per-iteration flags and lists.
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    pfast_status ensure(size_t bytes);
+    void release();
+    template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct PhaseTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+};
+
+}  // namespace pfast
+
+struct pfast_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    // device work buffers (reused across calls)
+    pfast::DevBuf s64, s32, T64, L64, scratch, mask, act, changed, ee, need, misc, grad_tmp, vp_tmp, picks_tmp;
+    pfast::DevBuf f2a, f2b, f2c;       // 2D field buffers
+    pfast::HostBuf h_act, h_changed, h_ee, h_need;
+    std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
+    std::map<std::pair<int, int>, pfast::DiagTable2> diag2;
+    cudaEvent_t ev[8] = {};
+    long long launches = 0;
+};
+
+struct pfast_survey3d {
+    pfast_ctx* ctx = nullptr;
+    int nz = 0, nr = 0, nc = 0;
+    double dx = 0, dy = 0, dz = 0;
+    int nsrc = 0, nrec = 0;
+    std::vector<int> h_src, h_srnum, h_ch0;
+    int* d_src_kij = nullptr;        // per source (k, i, j)
+    long long* d_src_lin = nullptr;  // per source linear node index
+    int* d_ch0 = nullptr;
+    int* d_srnum = nullptr;
+    int* d_rec = nullptr;
+    double* d_nxyz = nullptr;
+    double* d_tobs = nullptr;
+    unsigned char* d_last = nullptr;
+    bool has_picks = false;
+};
+
+struct pfast_survey2d {
+    pfast_ctx* ctx = nullptr;
+    int nr = 0, nc = 0;
+    double dx = 0, dz = 0;
+    int nsrc = 0, nrec = 0, numofr = 0;
+    std::vector<int> h_src, h_srnum, h_ch0;
+    std::vector<int> h_k2vec;         // [numofr][nc]: row of the last node above each reflector
+    std::vector<double> h_Z;
+    int* d_src_ij = nullptr;
+    int* d_ch0 = nullptr;
+    int* d_srnum = nullptr;
+    int* d_rec = nullptr;
+    double* d_nxy = nullptr;
+    double* d_ttobs = nullptr;
+    double* d_trobs = nullptr;
+    unsigned char* d_last_t = nullptr;   // last transmission-picked row at its node
+    unsigned char* d_last_r = nullptr;   // [nrec*numofr] last reflection-picked row at its node
+    double* d_Z = nullptr;
+    int* d_k2vec = nullptr;
+    bool has_picks = false;
+    int geom_status = 0;             // PFAST_ERR_NO_REFLECTION_POINT if a reflector has no node above it
+};
+
+namespace pfast {
+
+pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, DiagTable3** out);
+pfast_status ctx_diag2(pfast_ctx* ctx, int nr, int nc, DiagTable2** out);
+
+// The process-wide context of the calling thread's current device (reference shims).
+pfast_status default_context(pfast_ctx** out);
+
+// Time between two recorded events, added to *acc (ms).
+void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc);
+
+// Forward solve for sources [b0, b0+nb) of a 3D survey into ctx->T64 (FP64).
+pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, int nb, int precision, int maxswp,
+                             pfast_stats* st);
+// Adjoint for the same batch (T in ctx->T64): lambda into ctx->L64, EE per source into ee_out.
+pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, int nb, int precision, int maxswp,
+                             double* ee_out, pfast_stats* st);
+
+// 2D pipelines (engine2d.cu).
+pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, const pfast_options* opt,
+                            double* Tr, double* TTd_host, double* TTu_host, double* TT_host, pfast_stats* st);
+pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, const double* WR,
+                         const pfast_options* opt, double* gT, double* gR, double* gRT, double* Et, double* Er,
+                         pfast_stats* st);
+
+}  // namespace pfast

@@ -1,0 +1,82 @@
+// kernels.h -- host-side launchers of the pfast_gb300 CUDA kernels (internal).
+#pragma once
+
+#include <vector>
+#include "common.cuh"
+
+namespace pfast {
+
+// ------------------------------------------------------------------ 3D sweeps
+// Arguments of one tile-diagonal launch of a 3D sweep.  A "batch" holds
+// `nbatch` instances (sources) whose fields lie at field + inst*fstride.
+struct Sweep3Args {
+    void* field;              // Real fields, per instance
+    long long fstride;        // elements between instances (same for snap / aux / T)
+    const void* aux;          // forward: slowness (shared, Real); adjoint: T (double, per instance)
+    const unsigned* mask;     // adjoint: fixed-node bits, per instance, mask_stride words apart
+    long long mask_stride;
+    int wpr;                  // mask words per grid row
+    const int* src_kij;       // forward: per-instance source node (k, i, j)
+    void* snap;               // per-instance snapshot of the iteration start (Real)
+    int* changed;             // per-instance "an update exceeded the tolerance" flag
+    const int* act;           // active instance ids; grid.y indexes it
+    const int* diag_off;      // tile-diagonal table: tiles of diagonal d are
+    const unsigned* diag_tiles;  //   diag_tiles[diag_off[d] .. diag_off[d+1])
+    int nz, nr, nc;
+    int nbk, nbi, nbj;
+    Spacing3 sp;
+    int dir;                  // sweep order 0..7: bit2 = s3>0 (z), bit1 = s1>0 (rows), bit0 = s2>0 (cols)
+    int first, last;          // first / last sweep of an outer iteration
+    double tol_abs, tol_rel;  // change test: |new-old| > tol_abs + tol_rel*|new|
+};
+
+// Tile-diagonal table for a grid: tiles (bk, bi, bj) in flipped coordinates with
+// bk+bi+bj = d, packed bk | bi<<10 | bj<<20.
+struct DiagTable3 {
+    int nbk = 0, nbi = 0, nbj = 0, ndiag = 0;
+    std::vector<int> h_off;
+    int* d_off = nullptr;
+    unsigned* d_tiles = nullptr;
+};
+
+pfast_status build_diag_table3(int nz, int nr, int nc, DiagTable3& t);
+void free_diag_table3(DiagTable3& t);
+
+size_t sweep3_smem_bytes(int kind);
+pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
+
+// Small 3D kernels.
+pfast_status launch_slowness(const double* vp, double* s64, float* s32, long long n, cudaStream_t st);
+pfast_status launch_init_fwd3(void* field, int is_fp32, long long fstride, long long n, const long long* src_lin,
+                              int nbatch, cudaStream_t st);
+pfast_status launch_widen(const float* src, double* dst, long long fstride32, long long fstride64, long long n,
+                          int nbatch, cudaStream_t st);
+// lam64 <- lam32 for non-fixed nodes (fixed nodes keep their FP64 boundary value).
+pfast_status launch_widen_lambda(const float* l32, double* l64, const unsigned* mask, long long fstride32,
+                                 long long fstride64, long long mask_stride, int nz, int nr, int nc, int wpr,
+                                 int nbatch, cudaStream_t st);
+pfast_status launch_narrow(const double* src, float* dst, long long fstride64, long long fstride32, long long n,
+                           int nbatch, cudaStream_t st);
+
+// Receiver boundary condition + misfit (src/T_padjoint3d.h:90-127) for a batch of
+// sources.  rows of batch source b: [ch0[b], ch0[b]+srnum[b]); `last` marks the last
+// picked row at its node (earlier rows at the same node are overwritten by it in the
+// reference's sequential loop).
+struct Bc3Args {
+    const double* T; double* L; long long fstride;
+    unsigned* mask; long long mask_stride; int wpr;
+    const int* rec; const double* nxyz; const double* tobs; const unsigned char* last;
+    const int* ch0; const int* srnum; const int* src_kij;   // per batch source
+    double* EE; int* need;                                   // per batch source
+    int nz, nr, nc; double dx, dy, dz;
+};
+pfast_status launch_bc3(const Bc3Args& a, int nbatch, cudaStream_t st);
+
+// grad[n] <- grad[n] - lam_b[n] / (v*v*v), b = 0..nbatch-1 in order (src/T_PFAST3D.cpp:393).
+pfast_status launch_accumulate(double* grad, const double* lam, long long fstride, const double* vp, long long n,
+                               int nbatch, cudaStream_t st);
+// picks[row] = T_b[rec[row]] for rows of each batch source.
+pfast_status launch_gather3(const double* T, long long fstride, const int* rec, const int* ch0, const int* srnum,
+                            int nbatch, int nz, int nr, int nc, double* picks, cudaStream_t st);
+
+}  // namespace pfast

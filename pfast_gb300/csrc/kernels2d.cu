@@ -1,0 +1,602 @@
+// kernels2d.cu -- 2D fast-sweeping Eikonal (with Huygens reflection) and adjoint
+// kernels for sm_103a.
+//
+// Same scheme as the 3D kernels: the 4 sweep orders of the reference
+// (src/RT_pfsm2d.h:168-181, src/RT_padjoint2d.h:351-369) are run as wavefronts of
+// T2I x T2J tiles (one launch per tile anti-diagonal); inside a tile lane = row,
+// and step t updates the node anti-diagonal li + lj = t.  Upstream neighbours are
+// final and downstream ones untouched when a node is updated, exactly as in the
+// reference's lexicographic loop, so the plain FP64 flavour is bit-identical.
+
+#include <vector>
+#include <algorithm>
+#include "kernels2d.h"
+
+namespace pfast {
+
+namespace {
+
+template <int KIND> struct Traits2;
+template <> struct Traits2<kFwdPlain64>  { using Real = double; using Aux = double; static constexpr bool adj = false; };
+template <> struct Traits2<kFwdFast32>   { using Real = float;  using Aux = float;  static constexpr bool adj = false; };
+template <> struct Traits2<kFwdPolish64> { using Real = double; using Aux = double; static constexpr bool adj = false; };
+template <> struct Traits2<kAdjPlain64>  { using Real = double; using Aux = double; static constexpr bool adj = true; };
+template <> struct Traits2<kAdjFast32>   { using Real = float;  using Aux = float;  static constexpr bool adj = true; };
+template <> struct Traits2<kAdjPolish64> { using Real = double; using Aux = double; static constexpr bool adj = true; };
+
+template <int KIND>
+__host__ __device__ constexpr int warp_smem2() {
+    using T = Traits2<KIND>;
+    return int(H2I * R2 * sizeof(typename T::Real) + (T::adj ? H2I * R2 * sizeof(typename T::Aux) : 0));
+}
+
+__device__ __forceinline__ double ref_min(double x, double y) { return (x < y) ? x : y; }
+__device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
+
+// Reference 2D Godunov update (src/RT_pfsm2d.h:89-102), operand order kept.
+// a: x-neighbour minimum (spacing dx), b: z-neighbour minimum (dz).
+__device__ __forceinline__ double eik2_plain(double a, double b, double s, double dx, double dz, double i2x,
+                                             double i2z) {
+    double da = dx, db = dz, ia = i2x, ib = i2z, t;
+    if (b > a) { t = a; a = b; b = t; t = da; da = db; db = t; t = ia; ia = ib; ib = t; }
+    double q = b + db * s;
+    if (q <= a) return q;
+    const double A = ia + ib;   // 1.0/da/da + 1.0/db/db with each term precomputed as (1.0/d)/d
+    const double B = -2. * (a / da / da + b / db / db);
+    const double C = a * a / da / da + b * b / db / db - s * s;
+    const double D = B * B - 4 * A * C;
+    return (D >= 0) ? (-B + sqrt(D)) / 2. / A : kInf;
+}
+
+// Same solution in difference form: x = q - b, with B = a - b >= 0:
+//   1 term  x = db*s;  2 terms  x = (wa*B + sqrt((wa+wb) s^2 - wa wb B^2)) / (wa+wb)
+template <typename R>
+__device__ __forceinline__ R eik2_fast(R a, R b, R s, R dx, R dz, R wx, R wz, R rsum) {
+    R da = dx, db = dz, wa = wx, wb = wz, t;
+    if (b > a) { t = a; a = b; b = t; t = da; da = db; db = t; t = wa; wa = wb; wb = t; }
+    R q = fma(db, s, b);
+    if (q <= a) return q;
+    const R B = a - b;
+    const R waB = wa * B;
+    const R D = fma(wa + wb, s * s, -waB * wb * B);
+    return (D >= R(0)) ? b + (waB + sqrt(D)) * rsum : R(kInf);
+}
+
+__device__ __forceinline__ double pos_ref(double x) { return (x + fabs(x)) / 2.0; }
+__device__ __forceinline__ double neg_ref(double x) { return (x - fabs(x)) / 2.0; }
+
+// Reference 2D adjoint update (src/RT_padjoint2d.h:42-65).
+__device__ __forceinline__ double adj2_plain(double T0, double Txp, double Txm, double Tzp, double Tzm, double Lxp,
+                                             double Lxm, double Lzp, double Lzm, double dx, double dz) {
+    if (Txp >= kInf || T0 >= kInf || Txm >= kInf || Tzp >= kInf || Tzm >= kInf) return 0.0;
+    const double gxp = -(Txp - T0) / dx, gxm = -(T0 - Txm) / dx;
+    const double gzp = -(Tzp - T0) / dz, gzm = -(T0 - Tzm) / dz;
+    const double a1 = pos_ref(gxp), a2 = neg_ref(gxm);
+    const double b1 = pos_ref(gzp), b2 = neg_ref(gzm);
+    const double La1 = pos_ref(gxm) * Lxm, La2 = neg_ref(gxp) * Lxp;
+    const double Lb1 = pos_ref(gzm) * Lzm, Lb2 = neg_ref(gzp) * Lzp;
+    if (fabs((a1 - a2) / dx + (b1 - b2) / dz) > 1e-9)
+        return ((La1 - La2) / dx + (Lb1 - Lb2) / dz) / ((a1 - a2) / dx + (b1 - b2) / dz);
+    return 0.0;
+}
+
+template <typename R>
+__device__ __forceinline__ R adj2_fast(R T0, R Txp, R Txm, R Tzp, R Tzm, R Lxp, R Lxm, R Lzp, R Lzm, R rdx, R rdz,
+                                       R tinf) {
+    if (Txp >= tinf || T0 >= tinf || Txm >= tinf || Tzp >= tinf || Tzm >= tinf) return R(0);
+    const R gxp = (T0 - Txp) * rdx, gxm = (Txm - T0) * rdx;
+    const R gzp = (T0 - Tzp) * rdz, gzm = (Tzm - T0) * rdz;
+    const R z = R(0);
+    const R den = (fmax(gxp, z) - fmin(gxm, z)) * rdx + (fmax(gzp, z) - fmin(gzm, z)) * rdz;
+    if (!(fabs(den) > R(1e-9))) return z;
+    const R num = (fmax(gxm, z) * Lxm - fmin(gxp, z) * Lxp) * rdx + (fmax(gzm, z) * Lzm - fmin(gzp, z) * Lzp) * rdz;
+    return num / den;
+}
+
+template <typename Dst, typename Src, typename Conv>
+__device__ __forceinline__ void load_box2(Dst* box, const Src* __restrict__ g, int i0, int j0, int nr, int nc,
+                                          Dst fill, int lane, Conv conv) {
+    constexpr int NE = H2I * H2J;
+    constexpr int BATCH = 16;
+#pragma unroll 1
+    for (int base = 0; base < NE; base += 32 * BATCH) {
+        Dst v[BATCH];
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = base + u * 32 + lane;
+            v[u] = fill;
+            if (e < NE) {
+                const int y = e / H2J, x = e - y * H2J;
+                const int gi = i0 - 1 + y, gj = j0 - 1 + x;
+                if ((unsigned)gi < (unsigned)nr && (unsigned)gj < (unsigned)nc) v[u] = conv(g[(long long)gi * nc + gj]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = base + u * 32 + lane;
+            if (e < NE) {
+                const int y = e / H2J, x = e - y * H2J;
+                box[y * R2 + x] = v[u];
+            }
+        }
+    }
+}
+
+struct Ident2 {
+    template <typename T> __device__ __forceinline__ T operator()(T v) const { return v; }
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args A, const int d) {
+    using Real = typename Traits2<KIND>::Real;
+    using Aux = typename Traits2<KIND>::Aux;
+    constexpr bool ADJ = Traits2<KIND>::adj;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d0 = A.diag_off[d];
+    const int tile_idx = blockIdx.x * kWarps2 + warp;
+    if (tile_idx >= A.diag_off[d + 1] - d0) return;
+    const int q = A.act[blockIdx.y];
+
+    const unsigned pk = A.diag_tiles[d0 + tile_idx];
+    const bool py = A.dir & 2, px = A.dir & 1;
+    const int bif = pk & 0xffff, bjf = pk >> 16;
+    const int ti = py ? bif : A.nbi - 1 - bif;
+    const int tj = px ? bjf : A.nbj - 1 - bjf;
+    const int i0 = ti * T2I, j0 = tj * T2J;
+    const int nr = A.nr, nc = A.nc;
+    const int ei = min(T2I, nr - i0), ej = min(T2J, nc - j0);
+    const long long n = (long long)nr * nc;
+
+    Real* box = reinterpret_cast<Real*>(smem_raw + warp * warp_smem2<KIND>());
+    Aux* tbox = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + H2I * R2 * sizeof(Real));
+    Real* fld = reinterpret_cast<Real*>(A.field) + A.inst_off[q];
+    Real* snp = reinterpret_cast<Real*>(A.snap) + q * n;
+
+    const Real fill = ADJ ? Real(0) : Real(INFINITY);
+    load_box2(box, fld, i0, j0, nr, nc, fill, lane, Ident2());
+
+    const int lif = lane;
+    const bool lane_ok = lif < ei;
+    const int li = py ? lif : ei - 1 - lif;
+    const int gi = i0 + li;
+    unsigned fixed_lo = 0, fixed_hi = 0;
+    if constexpr (ADJ) {
+        const double* T = reinterpret_cast<const double*>(A.aux) + A.aux_off[q];
+        if constexpr (sizeof(Aux) == 8) {
+            load_box2(tbox, T, i0, j0, nr, nc, Aux(0), lane, Ident2());
+        } else {
+            double tr = T[(long long)i0 * nc + j0];
+            if (tr >= kInf) tr = 0.0;
+            load_box2(tbox, T, i0, j0, nr, nc, Aux(0), lane,
+                      [tr](double v) { return v >= kInf ? (Aux)INFINITY : (Aux)(v - tr); });
+        }
+        if (lane_ok) {
+            const unsigned* mrow = A.mask + A.mask_off[q] + (long long)gi * A.wpr + (j0 >> 5);
+            fixed_lo = mrow[0];
+            if ((j0 >> 5) + 1 < A.wpr) fixed_hi = mrow[1];
+        }
+    }
+
+    if (A.first) {
+        for (int y = 0; y < ei; ++y)
+            for (int x = lane; x < ej; x += 32) snp[(long long)(i0 + y) * nc + j0 + x] = box[(y + 1) * R2 + x + 1];
+    }
+    __syncwarp();
+
+    int lim_row = -1, si = -1, sj = -1;
+    if (A.inst_lim[q] >= 0) lim_row = A.inst_lim[q];
+    if (A.inst_src[q] >= 0) { si = A.inst_src[q] >> 16; sj = A.inst_src[q] & 0xffff; }
+    const int* rl = lim_row >= 0 ? A.rowlim + (long long)lim_row * nc : nullptr;
+    const Aux* slow = reinterpret_cast<const Aux*>(A.aux);
+    const bool row_interior = gi >= 1 && gi <= nr - 2;
+
+    const Real rdx = Real(1.0 / A.dx), rdz = Real(1.0 / A.dz);
+    const Real wx = Real(A.inv2x), wz = Real(A.inv2z);
+    const Real rsum = Real(1.0 / (A.inv2x + A.inv2z));
+    const int cb = (li + 1) * R2 + 1;
+    const int steps = ei + ej - 1;
+
+#pragma unroll 1
+    for (int t = 0; t < steps; ++t) {
+        const int ljf = t - lif;
+        if (lane_ok && ljf >= 0 && ljf < ej) {
+            const int lj = px ? ljf : ej - 1 - ljf;
+            const int c = cb + lj;
+            const int gj = j0 + lj;
+            if constexpr (!ADJ) {
+                const bool upd = (rl == nullptr || gi <= __ldg(rl + gj)) && !(gi == si && gj == sj);
+                if (upd) {
+                    const Real bz = ref_min(box[c - R2], box[c + R2]);
+                    const Real ax = ref_min(box[c + 1], box[c - 1]);
+                    const Real s = __ldg(slow + (long long)gi * nc + gj);
+                    if constexpr (KIND == kFwdPlain64) {
+                        const double qv = eik2_plain(ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z);
+                        box[c] = ref_min(box[c], qv);
+                    } else if constexpr (KIND == kFwdFast32) {
+                        const float qv = eik2_fast<float>(ax, bz, s, (float)A.dx, (float)A.dz, wx, wz, rsum);
+                        box[c] = ref_min(box[c], qv);
+                    } else {
+                        const double qv = eik2_fast<double>(ax, bz, s, A.dx, A.dz, wx, wz, rsum);
+                        if (qv < kInf) box[c] = qv;
+                    }
+                }
+            } else {
+                const unsigned fb = lj < 32 ? (fixed_lo >> lj) : (fixed_hi >> (lj - 32));
+                if (row_interior && gj >= 1 && gj <= nc - 2 && !(fb & 1u)) {
+                    Real r;
+                    if constexpr (KIND == kAdjPlain64) {
+                        r = adj2_plain(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
+                                       box[c - 1], box[c + R2], box[c - R2], A.dx, A.dz);
+                    } else {
+                        const Real tinf = (KIND == kAdjFast32) ? Real(INFINITY) : Real(kInf);
+                        r = adj2_fast<Real>(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
+                                            box[c - 1], box[c + R2], box[c - R2], rdx, rdz, tinf);
+                    }
+                    box[c] = r;
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    bool changed = false;
+    for (int y = 0; y < ei; ++y) {
+        for (int x = lane; x < ej; x += 32) {
+            const long long at = (long long)(i0 + y) * nc + j0 + x;
+            const Real v = box[(y + 1) * R2 + x + 1];
+            fld[at] = v;
+            if (A.last) {
+                const double diff = fabs((double)snp[at] - (double)v);
+                if (diff > A.tol_abs + A.tol_rel * fabs((double)v)) changed = true;
+            }
+        }
+    }
+    if (A.last && __any_sync(0xffffffffu, changed) && lane == 0) A.changed[q] = 1;
+}
+
+template <int KIND>
+pfast_status launch_one2(const Sweep2Args& a, int d, int tiles, int nact, cudaStream_t st) {
+    static bool attr_set = false;
+    const size_t smem = (size_t)kWarps2 * warp_smem2<KIND>();
+    if (!attr_set) {
+        PFAST_CUDA_TRY(cudaFuncSetAttribute(sweep2d_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    dim3 grid((tiles + kWarps2 - 1) / kWarps2, nact);
+    sweep2d_kernel<KIND><<<grid, kWarps2 * 32, smem, st>>>(a, d);
+    return PFAST_OK;
+}
+
+constexpr int kThreads = 256;
+
+__global__ void init2_kernel_d(double* base, const long long* off, const int* srcnode, long long n) {
+    const int q = blockIdx.y;
+    double* f = base + off[q];
+    const int sn = srcnode[q];
+    const long long s = sn >= 0 ? sn : -1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        f[t] = (t == s) ? 0.0 : kInf;
+}
+__global__ void init2_kernel_f(float* base, const long long* off, const int* srcnode, long long n) {
+    const int q = blockIdx.y;
+    float* f = base + off[q];
+    const int sn = srcnode[q];
+    const long long s = sn >= 0 ? sn : -1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        f[t] = (t == s) ? 0.0f : (float)kInf;
+}
+
+template <typename T>
+__global__ void copy_inst_kernel(const T* a, T* b, const long long* oa, const long long* ob, long long n) {
+    const int q = blockIdx.y;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        b[ob[q] + t] = a[oa[q] + t];
+}
+
+__global__ void widen_inst_kernel(const float* a, double* b, const long long* oa, const long long* ob, long long n) {
+    const int q = blockIdx.y;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        b[ob[q] + t] = (double)a[oa[q] + t];
+}
+
+__global__ void narrow_inst_kernel(const double* a, float* b, const long long* oa, const long long* ob, long long n) {
+    const int q = blockIdx.y;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        b[ob[q] + t] = (float)a[oa[q] + t];
+}
+
+__global__ void widen_lambda_inst_kernel(const float* a, double* b, const long long* oa, const long long* ob,
+                                         const unsigned* mask, const long long* mo, int nr, int nc, int wpr) {
+    const int q = blockIdx.y;
+    const long long n = (long long)nr * nc;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long i = t / nc;
+        const int j = (int)(t - i * nc);
+        if (!((mask[mo[q] + i * wpr + (j >> 5)] >> (j & 31)) & 1u)) b[ob[q] + t] = (double)a[oa[q] + t];
+    }
+}
+
+// One thread per (source, reflector) instance: the reflection points of one
+// reflector, columns in the reference's order, then the INF reset above them.
+__global__ void reflect2_kernel(const Reflect2Args A, int ninst) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ninst) return;
+    double* U = A.U + A.inst_off[q];
+    const int ir = A.inst_ir[q];
+    const int nc = A.nc, nr = A.nr;
+    const double dx = A.dx, dz = A.dz;
+    const int* k2r = A.k2 + (long long)ir * nc;
+    const int* qxc = A.qxcase + (long long)ir * nc;
+    const double* Zr = A.Z + (long long)ir * nc * 3;
+    for (int step = 0; step < nc; ++step) {
+        // interior columns 1..nc-2 first, then column 0, then column nc-1 (src/RT_pfsm2d.h:195,238,259)
+        const int jj = step < nc - 2 ? step + 1 : (step == nc - 2 ? 0 : nc - 1);
+        const int k2 = k2r[jj];
+        if (k2 < 0) continue;   // reflector below the model at this column: no reflection point
+        double qx;
+        const int cs = qxc[jj];
+        if (cs == 0) qx = (U[(long long)k2 * nc + jj + 1] - U[(long long)k2 * nc + jj - 1]) / 2.0 / dx;
+        else if (cs == 1) qx = (U[(long long)k2 * nc + jj] - U[(long long)k2 * nc + jj - 1]) / dx;
+        else qx = (U[(long long)k2 * nc + jj + 1] - U[(long long)k2 * nc + jj]) / dx;
+        const double u0 = U[(long long)k2 * nc + jj];
+        const double qz = (U[(long long)(k2 + 1) * nc + jj] - u0) / dz;
+        const double dnx = Zr[jj * 3 + 2], dnz = Zr[jj * 3 + 1], zd = Zr[jj * 3 + 0];
+        const double rz = qz - 2 * (qx * dnx + qz * dnz) * dnz;
+        const double v = u0 + qz * (zd - k2 * dz - dz) + rz * ((k2 + 1) * dz + dz - zd);
+        U[(long long)(k2 + 1) * nc + jj] = v;
+        if (v < 0) *A.err = 1;
+    }
+    for (int j = 0; j < nc; ++j) {
+        const int kv = A.k2vec[(long long)ir * nc + j];
+        for (int i = 0; i <= kv && i < nr; ++i) U[(long long)i * nc + j] = kInf;
+    }
+}
+
+// One warp per instance: receiver boundary condition and misfit, rows in order.
+__global__ void bc2_kernel(const Bc2Args A) {
+    const int q = blockIdx.x, lane = threadIdx.x;
+    const int s = A.inst_src[q], ir = A.inst_ir[q];
+    const double* T = A.T + A.t_off[q];
+    double* L = A.L + A.l_off[q];
+    unsigned* mask = A.mask + A.mask_off[q];
+    const int nc = A.nc, nr = A.nr;
+    const int r0 = A.ch0[s], nrec = A.srnum[s];
+    const int si = A.src_ij[2 * s], sj = A.src_ij[2 * s + 1];
+    const bool trans = ir < 0;
+    const double Cr = 1.0;
+    double E = A.EE[q];   // running misfit: the reflection adjoint keeps one sum over all reflectors
+    bool big = false;
+    for (int base = 0; base < nrec; base += 32) {
+        const int r = base + lane;
+        double e = 0.0;
+        if (r < nrec) {
+            const int row = r0 + r;
+            const double tob = trans ? A.ttobs[row] : A.trobs[(long long)row * A.numofr + ir];
+            const bool picked = trans ? (tob < 100) : (tob != 0);
+            if (picked) {
+                const int i = A.rec[2 * row], j = A.rec[2 * row + 1];
+                const long long o = (long long)i * nc + j;
+                atomicOr(&mask[(long long)i * A.wpr + (j >> 5)], 1u << (j & 31));
+                e = Cr * (tob - T[o]) * (tob - T[o]) / 2.0;
+                const bool last = trans ? A.last_t[row] : A.last_r[(long long)row * A.numofr + ir];
+                if (last && !(trans && i == si && j == sj)) {
+                    const double ny = A.nxy[2 * row], nx = A.nxy[2 * row + 1];
+                    const double Tz = (i + 1 >= nr) ? (T[o] - T[o - nc]) / A.dz : (T[o + nc] - T[o]) / A.dz;
+                    const double Tx = (j + 1 >= nc) ? (T[o] - T[o - 1]) / A.dx : (T[o + 1] - T[o]) / A.dx;
+                    double v = 0.0;
+                    if (fabs(tob - T[o]) > 1e-9 && fabs(nx * Tx + ny * Tz) > 1e-6) v = Cr * (tob - T[o]) / (nx * Tx + ny * Tz);
+                    L[o] = v;
+                    if (fabs(v) > kConvTol) big = true;
+                }
+            }
+        }
+        for (int l = 0; l < 32; ++l) {
+            const double el = __shfl_sync(0xffffffffu, e, l);
+            if (lane == 0) E += el;
+        }
+    }
+    big = __any_sync(0xffffffffu, big);
+    if (lane == 0) {
+        A.EE[q] = E;
+        A.need[q] = big ? 1 : 0;
+    }
+}
+
+__global__ void accumulate2_kernel(double* gT, double* gR, const double* lam, const long long* lo, const int* gslot,
+                                   const double* vp, long long n, int ninst) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double v = vp[t];
+        const double v3 = v * v * v;
+        double aT = gT[t], aR = gR[t];
+        for (int q = 0; q < ninst; ++q) {
+            const double x = lam[lo[q] + t] / v3;
+            if (gslot[q] == 0) aT = aT - x;
+            else aR = aR - x;
+        }
+        gT[t] = aT;
+        gR[t] = aR;
+    }
+}
+
+__global__ void blend2_kernel(const double* gT, const double* gR, const double* WR, double* gRT, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        gRT[t] = gT[t] * (1. - WR[t]) + gR[t] * WR[t];   // src/RT_PFAST2D.cpp:434
+}
+
+__global__ void addto2_kernel(double* dst, const long long* dof, const double* src, const long long* sof, long long n) {
+    const int q = blockIdx.y;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[dof[q] + t] = dst[dof[q] + t] + src[sof[q] + t];
+}
+
+__global__ void gather2_kernel(const double* fields, const long long* sfo, int numofr, long long n, const int* rec,
+                               const int* ch0, const int* srnum, int b0, int nc, double* Tr) {
+    const int b = blockIdx.y;
+    const int s = b0 + b;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < srnum[s]; r += gridDim.x * blockDim.x) {
+        const int row = ch0[s] + r;
+        const long long o = (long long)rec[2 * row] * nc + rec[2 * row + 1];
+        const double* base = fields + sfo[b];
+        Tr[(long long)row * (numofr + 1)] = base[o];
+        for (int ir = 0; ir < numofr; ++ir) Tr[(long long)row * (numofr + 1) + 1 + ir] = base[(1 + numofr + ir) * n + o];
+    }
+}
+
+inline unsigned grid_for(long long n, int ninst) {
+    long long b = (n + kThreads - 1) / kThreads;
+    long long cap = std::max(1LL, 152LL * 16 / std::max(1, ninst) + 1);
+    return (unsigned)std::max(1LL, std::min(b, cap));
+}
+
+}  // namespace
+
+#define PFAST_LAUNCH_CHECK2()                                                                 \
+    do {                                                                                      \
+        cudaError_t e__ = cudaGetLastError();                                                 \
+        if (e__ != cudaSuccess) return cuda_fail(e__, "kernel launch", __FILE__, __LINE__);   \
+    } while (0)
+
+pfast_status build_diag_table2(int nr, int nc, DiagTable2& t) {
+    t.nbi = (nr + T2I - 1) / T2I;
+    t.nbj = (nc + T2J - 1) / T2J;
+    if (t.nbi > 65535 || t.nbj > 65535) {
+        set_last_error("2D grid %dx%d too large", nr, nc);
+        return PFAST_ERR_INVALID;
+    }
+    t.ndiag = t.nbi + t.nbj - 1;
+    std::vector<unsigned> tiles;
+    t.h_off.assign(t.ndiag + 1, 0);
+    for (int d = 0; d < t.ndiag; ++d) {
+        t.h_off[d] = (int)tiles.size();
+        for (int bi = 0; bi < t.nbi; ++bi) {
+            const int bj = d - bi;
+            if (bj >= 0 && bj < t.nbj) tiles.push_back((unsigned)bi | ((unsigned)bj << 16));
+        }
+    }
+    t.h_off[t.ndiag] = (int)tiles.size();
+    PFAST_CUDA_TRY(cudaMalloc(&t.d_off, sizeof(int) * t.h_off.size()));
+    PFAST_CUDA_TRY(cudaMalloc(&t.d_tiles, sizeof(unsigned) * tiles.size()));
+    PFAST_CUDA_TRY(cudaMemcpy(t.d_off, t.h_off.data(), sizeof(int) * t.h_off.size(), cudaMemcpyHostToDevice));
+    PFAST_CUDA_TRY(cudaMemcpy(t.d_tiles, tiles.data(), sizeof(unsigned) * tiles.size(), cudaMemcpyHostToDevice));
+    return PFAST_OK;
+}
+
+void free_diag_table2(DiagTable2& t) {
+    if (t.d_off) cudaFree(t.d_off);
+    if (t.d_tiles) cudaFree(t.d_tiles);
+    t.d_off = nullptr;
+    t.d_tiles = nullptr;
+}
+
+pfast_status launch_sweep2(int kind, const Sweep2Args& a, int d, int tiles, int nact, cudaStream_t st) {
+    if (tiles <= 0 || nact <= 0) return PFAST_OK;
+    switch (kind) {
+        case kFwdPlain64: return launch_one2<kFwdPlain64>(a, d, tiles, nact, st);
+        case kFwdFast32: return launch_one2<kFwdFast32>(a, d, tiles, nact, st);
+        case kFwdPolish64: return launch_one2<kFwdPolish64>(a, d, tiles, nact, st);
+        case kAdjPlain64: return launch_one2<kAdjPlain64>(a, d, tiles, nact, st);
+        case kAdjFast32: return launch_one2<kAdjFast32>(a, d, tiles, nact, st);
+        case kAdjPolish64: return launch_one2<kAdjPolish64>(a, d, tiles, nact, st);
+    }
+    set_last_error("unknown sweep kind %d", kind);
+    return PFAST_ERR_INVALID;
+}
+
+pfast_status launch_init2(void* base, int is_fp32, const long long* off, const int* srcnode, long long n, int ninst,
+                          cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    dim3 grid(grid_for(n, ninst), ninst);
+    if (is_fp32) init2_kernel_f<<<grid, kThreads, 0, st>>>((float*)base, off, srcnode, n);
+    else init2_kernel_d<<<grid, kThreads, 0, st>>>((double*)base, off, srcnode, n);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_copy_inst(const void* src, void* dst, int is_fp32, const long long* os, const long long* od,
+                              long long n, int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    dim3 grid(grid_for(n, ninst), ninst);
+    if (is_fp32) copy_inst_kernel<float><<<grid, kThreads, 0, st>>>((const float*)src, (float*)dst, os, od, n);
+    else copy_inst_kernel<double><<<grid, kThreads, 0, st>>>((const double*)src, (double*)dst, os, od, n);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_widen_inst(const float* a, double* b, const long long* oa, const long long* ob, long long n,
+                               int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    dim3 grid(grid_for(n, ninst), ninst);
+    widen_inst_kernel<<<grid, kThreads, 0, st>>>(a, b, oa, ob, n);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_narrow_inst(const double* a, float* b, const long long* oa, const long long* ob, long long n,
+                                int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    dim3 grid(grid_for(n, ninst), ninst);
+    narrow_inst_kernel<<<grid, kThreads, 0, st>>>(a, b, oa, ob, n);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_widen_lambda_inst(const float* a, double* b, const long long* oa, const long long* ob,
+                                      const unsigned* mask, const long long* mo, int nr, int nc, int wpr, int ninst,
+                                      cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    dim3 grid(grid_for((long long)nr * nc, ninst), ninst);
+    widen_lambda_inst_kernel<<<grid, kThreads, 0, st>>>(a, b, oa, ob, mask, mo, nr, nc, wpr);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_reflect2(const Reflect2Args& a, int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    reflect2_kernel<<<(ninst + 63) / 64, 64, 0, st>>>(a, ninst);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_bc2(const Bc2Args& a, int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    bc2_kernel<<<ninst, 32, 0, st>>>(a);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_accumulate2(double* gT, double* gR, const double* lam, const long long* lo, const int* gslot,
+                                const double* vp, long long n, int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    accumulate2_kernel<<<grid_for(n, 1), kThreads, 0, st>>>(gT, gR, lam, lo, gslot, vp, n, ninst);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_blend2(const double* gT, const double* gR, const double* WR, double* gRT, long long n,
+                           cudaStream_t st) {
+    blend2_kernel<<<grid_for(n, 1), kThreads, 0, st>>>(gT, gR, WR, gRT, n);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_addto2(double* dst, const long long* dof, const double* src, const long long* sof, long long n,
+                           int ninst, cudaStream_t st) {
+    if (ninst <= 0) return PFAST_OK;
+    dim3 grid(grid_for(n, ninst), ninst);
+    addto2_kernel<<<grid, kThreads, 0, st>>>(dst, dof, src, sof, n);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+pfast_status launch_gather2(const double* fields, const long long* sfo, int numofr, long long n, const int* rec,
+                            const int* ch0, const int* srnum, int nbatch, int b0, int nc, double* Tr, cudaStream_t st) {
+    if (nbatch <= 0) return PFAST_OK;
+    dim3 grid(8, nbatch);
+    gather2_kernel<<<grid, kThreads, 0, st>>>(fields, sfo, numofr, n, rec, ch0, srnum, b0, nc, Tr);
+    PFAST_LAUNCH_CHECK2();
+    return PFAST_OK;
+}
+
+}  // namespace pfast

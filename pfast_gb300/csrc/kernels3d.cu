@@ -1,0 +1,633 @@
+// kernels3d.cu -- 3D fast-sweeping Eikonal and adjoint-state kernels for sm_103a.
+//
+// Sweep scheme.  The reference sweeps the grid lexicographically in 8 orders
+// (src/T_pfsm3d.h:158-178, src/T_padjoint3d.h:139-161).  In sweep order
+// (s3,s1,s2) a node sees its three upstream neighbours (k-s3, i-s1, j-s2) already
+// updated in this sweep and its three downstream neighbours not yet updated.  Any
+// visiting order with that property gives the same values, so this file visits
+// tiles on anti-diagonal tile hyperplanes (one launch per tile-diagonal, tiles of a
+// diagonal in parallel) and, inside a tile, nodes on anti-diagonal node hyperplanes
+// (one warp step per hyperplane).  The result of every node is the reference's.
+//
+// Flavours: kFwdPlain64 / kAdjPlain64 evaluate the reference's expressions in the
+// reference's order (the library is built with -fmad=false, so no FMA contraction):
+// bit-identical results.  kFwdFast32 / kAdjFast32 (bulk) and kFwdPolish64 /
+// kAdjPolish64 (polish) use the same Godunov / upwind-adjoint updates written with
+// precomputed reciprocals and a cancellation-free quadratic.
+
+#include <vector>
+#include <algorithm>
+#include "kernels.h"
+
+namespace pfast {
+
+namespace {
+
+template <int KIND> struct Traits;
+template <> struct Traits<kFwdPlain64>   { using Real = double; using Aux = double; static constexpr bool adj = false; };
+template <> struct Traits<kFwdFast32>    { using Real = float;  using Aux = float;  static constexpr bool adj = false; };
+template <> struct Traits<kFwdPolish64>  { using Real = double; using Aux = double; static constexpr bool adj = false; };
+template <> struct Traits<kAdjPlain64>   { using Real = double; using Aux = double; static constexpr bool adj = true; };
+template <> struct Traits<kAdjFast32>    { using Real = float;  using Aux = float;  static constexpr bool adj = true; };
+template <> struct Traits<kAdjPolish64>  { using Real = double; using Aux = double; static constexpr bool adj = true; };
+
+// Shared memory per warp: the field's halo box plus either the slowness tile
+// (forward) or the traveltime halo box (adjoint).
+template <int KIND>
+__host__ __device__ constexpr int warp_smem_bytes() {
+    using T = Traits<KIND>;
+    return int(HK * PS * sizeof(typename T::Real) +
+               (T::adj ? HK * PS * sizeof(typename T::Aux) : TK * SPS * sizeof(typename T::Aux)));
+}
+
+__device__ __forceinline__ double ref_min(double x, double y) { return (x < y) ? x : y; }  // MIN macro
+__device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
+
+// ----------------------------------------------------------- node updates
+// Reference Godunov update (src/T_pfsm3d.h:99-119).  a/b/c: neighbour minima along
+// x/y/z; s: slowness 1.0/vp (precomputed, bit-identical to the reference's per-node
+// division).  Expressions keep the reference's operand order.
+__device__ __forceinline__ double eik3_plain(double a, double b, double c, double s, const Spacing3& sp) {
+    double da = sp.d[0], db = sp.d[1], dc = sp.d[2];
+    double ia = sp.inv2[0], ib = sp.inv2[1], ic = sp.inv2[2];
+    double t;
+    if (b > a) { t = a; a = b; b = t; t = da; da = db; db = t; t = ia; ia = ib; ib = t; }
+    if (c > a) { t = a; a = c; c = t; t = da; da = dc; dc = t; t = ia; ia = ic; ic = t; }
+    if (c > b) { t = b; b = c; c = t; t = db; db = dc; dc = t; t = ib; ib = ic; ic = t; }
+    if (!(c <= b && b <= a)) return 0.0;
+    double q = dc * s + c;
+    if (q <= b) return q;
+    double A = dc * dc + db * db;
+    double B = -2. * (b * dc * dc + c * db * db);
+    double C = dc * dc * b * b + db * db * c * c - db * db * dc * dc * s * s;
+    double D = B * B - 4. * A * C;
+    q = (D >= 0) ? (-B + sqrt(D)) / 2. / A : kInf;
+    if (q <= a) return q;
+    A = ia + ib + ic;   // 1.0/da/da + 1.0/db/db + 1.0/dc/dc, each term precomputed as (1.0/d)/d
+    B = -2.0 * (a / da / da + b / db / db + c / dc / dc);
+    C = a * a / da / da + b * b / db / db + c * c / dc / dc - s * s;
+    D = B * B - 4. * A * C;
+    q = (D >= 0) ? (-B + sqrt(D)) / 2. / A : kInf;
+    return q;
+}
+
+// Constants of the fast Godunov form: w = 1/d^2 per axis, rp[ax] = 1/(W - w[ax]) (the
+// pair of the two other axes), rW = 1/W with W = sum w.
+template <typename R> struct FastConst {
+    R d[3], w[3], rp[3], rW;
+};
+
+template <typename R>
+__device__ __forceinline__ FastConst<R> fast_const(const Spacing3& sp) {
+    FastConst<R> k;
+    double W = sp.inv2[0] + sp.inv2[1] + sp.inv2[2];
+    for (int a = 0; a < 3; ++a) {
+        k.d[a] = (R)sp.d[a];
+        k.w[a] = (R)sp.inv2[a];
+        k.rp[a] = (R)(1.0 / (W - sp.inv2[a]));
+    }
+    k.rW = (R)(1.0 / W);
+    return k;
+}
+
+// Same Godunov solution as eik3_plain, in difference form relative to the smallest
+// neighbour c (x = q - c), with FMA and reciprocal multiplies:
+//   1 term:  x = dc*s
+//   2 terms: x = (wb*B + sqrt((wb+wc) s^2 - wb wc B^2)) / (wb+wc),         B = b-c
+//   3 terms: x = (wa*A + wb*B + sqrt(W s^2 - wa wb (A-B)^2 - wa wc A^2 - wb wc B^2)) / W,  A = a-c
+template <typename R>
+__device__ __forceinline__ R eik3_fast(R a, R b, R c, R s, const FastConst<R>& K) {
+    R da = K.d[0], db = K.d[1], dc = K.d[2];
+    R wa = K.w[0], wb = K.w[1], wc = K.w[2];
+    R ra = K.rp[0], rb = K.rp[1], rc = K.rp[2];
+    R t;
+    if (b > a) { t = a; a = b; b = t; t = da; da = db; db = t; t = wa; wa = wb; wb = t; t = ra; ra = rb; rb = t; }
+    if (c > a) { t = a; a = c; c = t; t = da; da = dc; dc = t; t = wa; wa = wc; wc = t; t = ra; ra = rc; rc = t; }
+    if (c > b) { t = b; b = c; c = t; t = db; db = dc; dc = t; t = wb; wb = wc; wc = t; t = rb; rb = rc; rc = t; }
+    R q = fma(dc, s, c);
+    if (q <= b) return q;
+    const R s2 = s * s;
+    const R B = b - c;
+    const R wbB = wb * B;
+    R D = fma(wb + wc, s2, -wbB * wc * B);
+    q = (D >= R(0)) ? c + (wbB + sqrt(D)) * ra : R(kInf);
+    if (q <= a) return q;
+    const R A = a - c;
+    const R AB = A - B;
+    const R W = wa + wb + wc;
+    R D3 = W * s2 - (wa * wb * AB * AB + wa * wc * A * A + wb * wc * B * B);
+    q = (D3 >= R(0)) ? c + (fma(wa, A, wbB) + sqrt(D3)) * K.rW : R(kInf);
+    return q;
+}
+
+__device__ __forceinline__ double pos_ref(double x) { return (x + fabs(x)) / 2.0; }   // POS macro
+__device__ __forceinline__ double neg_ref(double x) { return (x - fabs(x)) / 2.0; }   // NEG macro
+
+// Reference adjoint update (src/T_padjoint3d.h:42-71); operand order kept.
+__device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, double Typ, double Tym,
+                                             double Tzp, double Tzm, double Lxp, double Lxm, double Lyp,
+                                             double Lym, double Lzp, double Lzm, const Spacing3& sp) {
+    if (T0 >= kInf || Txp >= kInf || Txm >= kInf || Typ >= kInf || Tym >= kInf || Tzp >= kInf || Tzm >= kInf)
+        return 0.0;
+    const double dx = sp.d[0], dy = sp.d[1], dz = sp.d[2];
+    const double gxp = -(Txp - T0) / dx, gxm = -(T0 - Txm) / dx;
+    const double gyp = -(Typ - T0) / dy, gym = -(T0 - Tym) / dy;
+    const double gzp = -(Tzp - T0) / dz, gzm = -(T0 - Tzm) / dz;
+    const double a1 = pos_ref(gxp), a2 = neg_ref(gxm);
+    const double b1 = pos_ref(gyp), b2 = neg_ref(gym);
+    const double c1 = pos_ref(gzp), c2 = neg_ref(gzm);
+    const double La1 = pos_ref(gxm) * Lxm, La2 = neg_ref(gxp) * Lxp;
+    const double Lb1 = pos_ref(gym) * Lym, Lb2 = neg_ref(gyp) * Lyp;
+    const double Lc1 = pos_ref(gzm) * Lzm, Lc2 = neg_ref(gzp) * Lzp;
+    const double den = (a1 - a2) / dx + (b1 - b2) / dy + (c1 - c2) / dz;
+    if (fabs(den) > 1e-9) return ((La1 - La2) / dx + (Lb1 - Lb2) / dy + (Lc1 - Lc2) / dz) / den;
+    return 0.0;
+}
+
+// Fast adjoint update: the same upwind formula with reciprocal multiplies.  T
+// values may be offsets from a common reference (differences are unchanged);
+// an unreached neighbour is marked by T >= tinf.
+template <typename R>
+__device__ __forceinline__ R adj3_fast(R T0, R Txp, R Txm, R Typ, R Tym, R Tzp, R Tzm, R Lxp, R Lxm, R Lyp,
+                                       R Lym, R Lzp, R Lzm, R rdx, R rdy, R rdz, R tinf) {
+    if (T0 >= tinf || Txp >= tinf || Txm >= tinf || Typ >= tinf || Tym >= tinf || Tzp >= tinf || Tzm >= tinf)
+        return R(0);
+    const R gxp = (T0 - Txp) * rdx, gxm = (Txm - T0) * rdx;
+    const R gyp = (T0 - Typ) * rdy, gym = (Tym - T0) * rdy;
+    const R gzp = (T0 - Tzp) * rdz, gzm = (Tzm - T0) * rdz;
+    const R z = R(0);
+    const R den = (fmax(gxp, z) - fmin(gxm, z)) * rdx + (fmax(gyp, z) - fmin(gym, z)) * rdy +
+                  (fmax(gzp, z) - fmin(gzm, z)) * rdz;
+    if (!(fabs(den) > R(1e-9))) return z;
+    const R num = (fmax(gxm, z) * Lxm - fmin(gxp, z) * Lxp) * rdx + (fmax(gym, z) * Lym - fmin(gyp, z) * Lyp) * rdy +
+                  (fmax(gzm, z) * Lzm - fmin(gzp, z) * Lzp) * rdz;
+    return num / den;
+}
+
+// ----------------------------------------------------------- tile I/O
+// Load the (TK+2)x(TI+2)x(TJ+2) halo box at origin (k0-1, i0-1, j0-1) into `box`
+// (plane stride PS, row stride HJ).  Out-of-grid entries get `fill`.  Loads are
+// issued 16 per lane before their shared-memory stores, to keep many in flight.
+template <typename Dst, typename Src, typename Conv>
+__device__ __forceinline__ void load_box(Dst* box, const Src* __restrict__ g, int k0, int i0, int j0, int nz, int nr,
+                                         int nc, Dst fill, int lane, Conv conv) {
+    constexpr int NE = HK * HI * HJ;
+    constexpr int BATCH = 16;
+    const long long plane = (long long)nr * nc;
+#pragma unroll 1
+    for (int base = 0; base < NE; base += 32 * BATCH) {
+        Dst v[BATCH];
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = base + u * 32 + lane;
+            v[u] = fill;
+            if (e < NE) {
+                const int r = e / HJ, x = e - r * HJ;
+                const int z = r / HI, y = r - z * HI;
+                const int gk = k0 - 1 + z, gi = i0 - 1 + y, gj = j0 - 1 + x;
+                if ((unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr && (unsigned)gj < (unsigned)nc)
+                    v[u] = conv(g[gk * plane + (long long)gi * nc + gj]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = base + u * 32 + lane;
+            if (e < NE) {
+                const int r = e / HJ, x = e - r * HJ;
+                const int z = r / HI, y = r - z * HI;
+                box[z * PS + y * HJ + x] = v[u];
+            }
+        }
+    }
+}
+
+struct Ident {
+    template <typename T> __device__ __forceinline__ T operator()(T v) const { return v; }
+};
+
+// ----------------------------------------------------------- the sweep kernel
+template <int KIND>
+__global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args A, const int d) {
+    using Real = typename Traits<KIND>::Real;
+    using Aux = typename Traits<KIND>::Aux;
+    constexpr bool ADJ = Traits<KIND>::adj;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d0 = A.diag_off[d];
+    const int tile_idx = blockIdx.x * kWarps3 + warp;
+    if (tile_idx >= A.diag_off[d + 1] - d0) return;
+    const int inst = A.act[blockIdx.y];
+
+    // ---- tile placement (the diagonal table is in flipped coordinates)
+    const unsigned pk = A.diag_tiles[d0 + tile_idx];
+    const bool pz = A.dir & 4, py = A.dir & 2, px = A.dir & 1;
+    const int bkf = pk & 1023, bif = (pk >> 10) & 1023, bjf = pk >> 20;
+    const int tk = pz ? bkf : A.nbk - 1 - bkf;
+    const int ti = py ? bif : A.nbi - 1 - bif;
+    const int tj = px ? bjf : A.nbj - 1 - bjf;
+    const int k0 = tk * TK, i0 = ti * TI, j0 = tj * TJ;
+    const int ek = min(TK, A.nz - k0), ei = min(TI, A.nr - i0), ej = min(TJ, A.nc - j0);
+    const int nz = A.nz, nr = A.nr, nc = A.nc;
+    const long long plane = (long long)nr * nc;
+
+    Real* box = reinterpret_cast<Real*>(smem_raw + warp * warp_smem_bytes<KIND>());
+    Aux* aux = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
+    Real* fld = reinterpret_cast<Real*>(A.field) + inst * A.fstride;
+    Real* snp = reinterpret_cast<Real*>(A.snap) + inst * A.fstride;
+
+    // ---- stage the field halo box (out-of-grid: +inf for the forward so that the
+    // neighbour minimum reduces to the one-sided rule at faces; never read by the adjoint)
+    const Real fill = ADJ ? Real(0) : Real(INFINITY);
+    load_box(box, fld, k0, i0, j0, nz, nr, nc, fill, lane, Ident());
+
+    // ---- auxiliary data
+    double tref = 0.0;
+    unsigned fixed_bits = 0;
+    const int lkf = lane / TI, lif = lane % TI;
+    const bool lane_ok = lkf < ek && lif < ei;
+    const int lk = pz ? lkf : ek - 1 - lkf;
+    const int li = py ? lif : ei - 1 - lif;
+    if constexpr (!ADJ) {
+        // slowness tile [lk][li][lj], rows loaded coalesced
+        const Aux* s = reinterpret_cast<const Aux*>(A.aux);
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
+            const int rk = m / TI, ri = m % TI;
+            if (rk < ek && ri < ei && lane < ej)
+                aux[rk * SPS + ri * SJ + lane] = s[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane];
+        }
+    } else {
+        const double* T = reinterpret_cast<const double*>(A.aux) + inst * A.fstride;
+        if constexpr (sizeof(Aux) == 8) {
+            load_box(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane, Ident());
+        } else {
+            // FP32 bulk: offsets from one reference time of the tile keep the
+            // differences accurate; unreached nodes become +inf
+            tref = T[(long long)k0 * plane + (long long)i0 * nc + j0];
+            if (tref >= kInf) tref = 0.0;
+            const double tr = tref;
+            load_box(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane,
+                     [tr](double v) { return v >= kInf ? (Aux)INFINITY : (Aux)(v - tr); });
+        }
+        if (lane_ok)
+            fixed_bits = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
+    }
+
+    // ---- snapshot of the iteration start (first sweep of an outer iteration)
+    if (A.first) {
+#pragma unroll 4
+        for (int m = 0; m < 32; ++m) {
+            const int rk = m / TI, ri = m % TI;
+            if (rk < ek && ri < ei && lane < ej)
+                snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
+                    box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+        }
+    }
+    __syncwarp();
+
+    // ---- wavefront over the tile's node hyperplanes
+    const int gk = k0 + lk, gi = i0 + li;
+    const int cbase = (lk + 1) * PS + (li + 1) * HJ + 1;
+    const int steps = ek + ei + ej - 2;
+    int sk = -1, si = -1, sj = -1;
+    if constexpr (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
+    const bool row_interior = ADJ ? (gk >= 1 && gk <= nz - 2 && gi >= 1 && gi <= nr - 2) : true;
+
+    FastConst<Real> K;
+    if constexpr (KIND == kFwdFast32 || KIND == kFwdPolish64) K = fast_const<Real>(A.sp);
+    const Real rdx = Real(1.0 / A.sp.d[0]), rdy = Real(1.0 / A.sp.d[1]), rdz = Real(1.0 / A.sp.d[2]);
+
+#pragma unroll 1
+    for (int t = 0; t < steps; ++t) {
+        const int ljf = t - lkf - lif;
+        if (lane_ok && ljf >= 0 && ljf < ej) {
+            const int lj = px ? ljf : ej - 1 - ljf;
+            const int c = cbase + lj;
+            const int gj = j0 + lj;
+            if constexpr (!ADJ) {
+                if (!(gk == sk && gi == si && gj == sj)) {
+                    const Real xa = ref_min(box[c + 1], box[c - 1]);
+                    const Real yb = ref_min(box[c - HJ], box[c + HJ]);
+                    const Real zc = ref_min(box[c - PS], box[c + PS]);
+                    const Real s = aux[lk * SPS + li * SJ + lj];
+                    if constexpr (KIND == kFwdPlain64) {
+                        const double q = eik3_plain(xa, yb, zc, s, A.sp);
+                        box[c] = ref_min(box[c], q);
+                    } else if constexpr (KIND == kFwdFast32) {
+                        const float q = eik3_fast<float>(xa, yb, zc, s, K);
+                        box[c] = ref_min(box[c], q);
+                    } else {   // polish: the Godunov value itself, unless unreachable
+                        const double q = eik3_fast<double>(xa, yb, zc, s, K);
+                        if (q < kInf) box[c] = q;
+                    }
+                }
+            } else {
+                if (row_interior && gj >= 1 && gj <= nc - 2 && !((fixed_bits >> lj) & 1u)) {
+                    Real r;
+                    if constexpr (KIND == kAdjPlain64) {
+                        r = adj3_plain(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                       aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
+                                       box[c - PS], A.sp);
+                    } else {
+                        const Real tinf = (KIND == kAdjFast32) ? Real(INFINITY) : Real(kInf);
+                        r = adj3_fast<Real>(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                            aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ],
+                                            box[c + PS], box[c - PS], rdx, rdy, rdz, tinf);
+                    }
+                    box[c] = r;
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    // ---- write back; on the last sweep compare with the iteration-start snapshot
+    bool changed = false;
+#pragma unroll 4
+    for (int m = 0; m < 32; ++m) {
+        const int rk = m / TI, ri = m % TI;
+        if (rk < ek && ri < ei && lane < ej) {
+            const long long at = (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane;
+            const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+            fld[at] = v;
+            if (A.last) {
+                const Real p = snp[at];
+                const double diff = fabs((double)p - (double)v);
+                if (diff > A.tol_abs + A.tol_rel * fabs((double)v)) changed = true;
+            }
+        }
+    }
+    if (A.last && __any_sync(0xffffffffu, changed) && lane == 0) A.changed[inst] = 1;
+    (void)tref;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ tables
+pfast_status build_diag_table3(int nz, int nr, int nc, DiagTable3& t) {
+    t.nbk = (nz + TK - 1) / TK;
+    t.nbi = (nr + TI - 1) / TI;
+    t.nbj = (nc + TJ - 1) / TJ;
+    if (t.nbk > 1023 || t.nbi > 1023 || t.nbj > 1023) {
+        set_last_error("grid %dx%dx%d too large for the tile table", nz, nr, nc);
+        return PFAST_ERR_INVALID;
+    }
+    t.ndiag = t.nbk + t.nbi + t.nbj - 2;
+    std::vector<unsigned> tiles;
+    t.h_off.assign(t.ndiag + 1, 0);
+    for (int dd = 0; dd < t.ndiag; ++dd) {
+        t.h_off[dd] = (int)tiles.size();
+        for (int bk = 0; bk < t.nbk; ++bk)
+            for (int bi = 0; bi < t.nbi; ++bi) {
+                const int bj = dd - bk - bi;
+                if (bj >= 0 && bj < t.nbj) tiles.push_back((unsigned)bk | ((unsigned)bi << 10) | ((unsigned)bj << 20));
+            }
+    }
+    t.h_off[t.ndiag] = (int)tiles.size();
+    PFAST_CUDA_TRY(cudaMalloc(&t.d_off, sizeof(int) * t.h_off.size()));
+    PFAST_CUDA_TRY(cudaMalloc(&t.d_tiles, sizeof(unsigned) * tiles.size()));
+    PFAST_CUDA_TRY(cudaMemcpy(t.d_off, t.h_off.data(), sizeof(int) * t.h_off.size(), cudaMemcpyHostToDevice));
+    PFAST_CUDA_TRY(cudaMemcpy(t.d_tiles, tiles.data(), sizeof(unsigned) * tiles.size(), cudaMemcpyHostToDevice));
+    return PFAST_OK;
+}
+
+void free_diag_table3(DiagTable3& t) {
+    if (t.d_off) cudaFree(t.d_off);
+    if (t.d_tiles) cudaFree(t.d_tiles);
+    t.d_off = nullptr;
+    t.d_tiles = nullptr;
+}
+
+size_t sweep3_smem_bytes(int kind) {
+    switch (kind) {
+        case kFwdPlain64: return (size_t)kWarps3 * warp_smem_bytes<kFwdPlain64>();
+        case kFwdFast32: return (size_t)kWarps3 * warp_smem_bytes<kFwdFast32>();
+        case kFwdPolish64: return (size_t)kWarps3 * warp_smem_bytes<kFwdPolish64>();
+        case kAdjPlain64: return (size_t)kWarps3 * warp_smem_bytes<kAdjPlain64>();
+        case kAdjFast32: return (size_t)kWarps3 * warp_smem_bytes<kAdjFast32>();
+        case kAdjPolish64: return (size_t)kWarps3 * warp_smem_bytes<kAdjPolish64>();
+    }
+    return 0;
+}
+
+template <int KIND>
+static pfast_status launch_one(const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st) {
+    static bool attr_set = false;
+    const size_t smem = (size_t)kWarps3 * warp_smem_bytes<KIND>();
+    if (!attr_set) {
+        PFAST_CUDA_TRY(cudaFuncSetAttribute(sweep3d_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    dim3 grid((tiles + kWarps3 - 1) / kWarps3, nact);
+    sweep3d_kernel<KIND><<<grid, kWarps3 * 32, smem, st>>>(a, d);
+    return PFAST_OK;
+}
+
+pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st) {
+    if (tiles <= 0 || nact <= 0) return PFAST_OK;
+    switch (kind) {
+        case kFwdPlain64: return launch_one<kFwdPlain64>(a, d, tiles, nact, st);
+        case kFwdFast32: return launch_one<kFwdFast32>(a, d, tiles, nact, st);
+        case kFwdPolish64: return launch_one<kFwdPolish64>(a, d, tiles, nact, st);
+        case kAdjPlain64: return launch_one<kAdjPlain64>(a, d, tiles, nact, st);
+        case kAdjFast32: return launch_one<kAdjFast32>(a, d, tiles, nact, st);
+        case kAdjPolish64: return launch_one<kAdjPolish64>(a, d, tiles, nact, st);
+    }
+    set_last_error("unknown sweep kind %d", kind);
+    return PFAST_ERR_INVALID;
+}
+
+// ------------------------------------------------------------------ small kernels
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(long long n) {
+    long long b = (n + kThreads - 1) / kThreads;
+    return (unsigned)std::min<long long>(b, 152LL * 64);
+}
+
+__global__ void slowness_kernel(const double* __restrict__ vp, double* __restrict__ s64, float* __restrict__ s32,
+                                long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double s = 1.0 / vp[t];   // s = 1.0/vp, src/T_pfsm3d.h:75
+        s64[t] = s;
+        if (s32) s32[t] = (float)s;
+    }
+}
+
+template <typename Real>
+__global__ void init_fwd_kernel(Real* __restrict__ f, long long fstride, long long n, const long long* __restrict__ src_lin) {
+    const int b = blockIdx.y;
+    Real* g = f + b * fstride;
+    const long long sn = src_lin[b];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        g[t] = (t == sn) ? Real(0) : Real(kInf);   // point-source initialisation, src/T_pfsm3d.h:139-148
+}
+
+__global__ void widen_kernel(const float* __restrict__ a, double* __restrict__ b, long long s32, long long s64, long long n) {
+    const int k = blockIdx.y;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        b[k * s64 + t] = (double)a[k * s32 + t];
+}
+
+__global__ void narrow_kernel(const double* __restrict__ a, float* __restrict__ b, long long s64, long long s32, long long n) {
+    const int k = blockIdx.y;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        b[k * s32 + t] = (float)a[k * s64 + t];
+}
+
+__global__ void widen_lambda_kernel(const float* __restrict__ a, double* __restrict__ b, const unsigned* __restrict__ mask,
+                                    long long s32, long long s64, long long ms, int nz, int nr, int nc, int wpr) {
+    const int k = blockIdx.y;
+    const long long n = (long long)nz * nr * nc;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long row = t / nc;
+        const int j = (int)(t - row * nc);
+        const bool fixed = (mask[k * ms + row * wpr + (j >> 5)] >> (j & 31)) & 1u;
+        if (!fixed) b[k * s64 + t] = (double)a[k * s32 + t];
+    }
+}
+
+// One warp per source.  Lanes evaluate 32 consecutive receiver rows; the misfit is
+// summed by lane 0 in row order (the reference's EE += ... sequence).
+__global__ void bc3_kernel(const Bc3Args A) {
+    const int b = blockIdx.x;
+    const int lane = threadIdx.x;
+    const double* T = A.T + b * A.fstride;
+    double* L = A.L + b * A.fstride;
+    unsigned* mask = A.mask + b * A.mask_stride;
+    const long long plane = (long long)A.nr * A.nc;
+    const int r0 = A.ch0[b], nrec = A.srnum[b];
+    const int sk = A.src_kij[3 * b], si = A.src_kij[3 * b + 1], sj = A.src_kij[3 * b + 2];
+    double E = 0.0;
+    bool big = false;
+    for (int base = 0; base < nrec; base += 32) {
+        const int r = base + lane;
+        double e = 0.0;
+        if (r < nrec) {
+            const int row = r0 + r;
+            const double tob = A.tobs[row];
+            if (tob < 100) {   // only picked first arrivals, src/T_padjoint3d.h:95
+                const int i = A.rec[3 * row], j = A.rec[3 * row + 1], k = A.rec[3 * row + 2];
+                const long long o = k * plane + (long long)i * A.nc + j;
+                atomicOr(&mask[((long long)k * A.nr + i) * A.wpr + (j >> 5)], 1u << (j & 31));
+                const double res = tob - T[o];
+                e = res * res / 2.0;
+                if (A.last[row] && !(i == si && j == sj && k == sk)) {
+                    const double ny = A.nxyz[3 * row], nx = A.nxyz[3 * row + 1], nzz = A.nxyz[3 * row + 2];
+                    const double Tz = (k + 1 >= A.nz) ? (T[o] - T[o - plane]) / A.dz : (T[o + plane] - T[o]) / A.dz;
+                    const double Ty = (i + 1 >= A.nr) ? (T[o] - T[o - A.nc]) / A.dy : (T[o + A.nc] - T[o]) / A.dy;
+                    const double Tx = (j + 1 >= A.nc) ? (T[o] - T[o - 1]) / A.dx : (T[o + 1] - T[o]) / A.dx;
+                    double v = 0.0;
+                    if (fabs(tob - T[o]) > 1e-9 && fabs(nx * Tx + ny * Ty + nzz * Tz) > 1e-6)
+                        v = (tob - T[o]) / (nx * Tx + ny * Ty + nzz * Tz);
+                    L[o] = v;
+                    if (fabs(v) > kConvTol) big = true;
+                }
+            }
+        }
+        for (int l = 0; l < 32; ++l) {
+            const double el = __shfl_sync(0xffffffffu, e, l);
+            if (lane == 0) E += el;   // adding 0 for unpicked rows leaves E unchanged
+        }
+    }
+    big = __any_sync(0xffffffffu, big);
+    if (lane == 0) {
+        A.EE[b] = E;
+        A.need[b] = big ? 1 : 0;   // first isconv(p=0, U) test of src/T_padjoint3d.h:135
+    }
+}
+
+__global__ void accumulate_kernel(double* __restrict__ g, const double* __restrict__ lam, long long fstride,
+                                  const double* __restrict__ vp, long long n, int nb) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double v = vp[t];
+        const double v3 = v * v * v;
+        double acc = g[t];
+        for (int b = 0; b < nb; ++b) acc = acc - lam[b * fstride + t] / v3;   // src/T_PFAST3D.cpp:393
+        g[t] = acc;
+    }
+}
+
+__global__ void gather3_kernel(const double* __restrict__ T, long long fstride, const int* __restrict__ rec,
+                               const int* __restrict__ ch0, const int* __restrict__ srnum, int nz, int nr, int nc,
+                               double* __restrict__ picks) {
+    const int b = blockIdx.y;
+    const long long plane = (long long)nr * nc;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < srnum[b]; r += gridDim.x * blockDim.x) {
+        const int row = ch0[b] + r;
+        const int i = rec[3 * row], j = rec[3 * row + 1], k = rec[3 * row + 2];
+        picks[row] = T[b * fstride + k * plane + (long long)i * nc + j];
+    }
+}
+
+}  // namespace
+
+#define PFAST_LAUNCH_CHECK()                                                                   \
+    do {                                                                                       \
+        cudaError_t e__ = cudaGetLastError();                                                  \
+        if (e__ != cudaSuccess) return cuda_fail(e__, "kernel launch", __FILE__, __LINE__);    \
+    } while (0)
+
+pfast_status launch_slowness(const double* vp, double* s64, float* s32, long long n, cudaStream_t st) {
+    slowness_kernel<<<grid_for(n), kThreads, 0, st>>>(vp, s64, s32, n);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_init_fwd3(void* field, int is_fp32, long long fstride, long long n, const long long* src_lin,
+                              int nbatch, cudaStream_t st) {
+    dim3 grid(std::max(1u, grid_for(n) / std::max(1, nbatch / 8 + 1)), nbatch);
+    if (is_fp32) init_fwd_kernel<float><<<grid, kThreads, 0, st>>>((float*)field, fstride, n, src_lin);
+    else init_fwd_kernel<double><<<grid, kThreads, 0, st>>>((double*)field, fstride, n, src_lin);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_widen(const float* a, double* b, long long s32, long long s64, long long n, int nbatch, cudaStream_t st) {
+    dim3 grid(std::max(1u, grid_for(n) / std::max(1, nbatch / 8 + 1)), nbatch);
+    widen_kernel<<<grid, kThreads, 0, st>>>(a, b, s32, s64, n);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_narrow(const double* a, float* b, long long s64, long long s32, long long n, int nbatch, cudaStream_t st) {
+    dim3 grid(std::max(1u, grid_for(n) / std::max(1, nbatch / 8 + 1)), nbatch);
+    narrow_kernel<<<grid, kThreads, 0, st>>>(a, b, s64, s32, n);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_widen_lambda(const float* l32, double* l64, const unsigned* mask, long long s32, long long s64,
+                                 long long ms, int nz, int nr, int nc, int wpr, int nbatch, cudaStream_t st) {
+    const long long n = (long long)nz * nr * nc;
+    dim3 grid(std::max(1u, grid_for(n) / std::max(1, nbatch / 8 + 1)), nbatch);
+    widen_lambda_kernel<<<grid, kThreads, 0, st>>>(l32, l64, mask, s32, s64, ms, nz, nr, nc, wpr);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_bc3(const Bc3Args& a, int nbatch, cudaStream_t st) {
+    bc3_kernel<<<nbatch, 32, 0, st>>>(a);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_accumulate(double* grad, const double* lam, long long fstride, const double* vp, long long n,
+                               int nbatch, cudaStream_t st) {
+    accumulate_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, lam, fstride, vp, n, nbatch);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_gather3(const double* T, long long fstride, const int* rec, const int* ch0, const int* srnum,
+                            int nbatch, int nz, int nr, int nc, double* picks, cudaStream_t st) {
+    dim3 grid(16, nbatch);
+    gather3_kernel<<<grid, kThreads, 0, st>>>(T, fstride, rec, ch0, srnum, nz, nr, nc, picks);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+}  // namespace pfast

@@ -1,0 +1,150 @@
+"""2D parity on the GPU (RT_fsm2d with Huygens reflection, transmission and
+reflection adjoints, joint gradient) through the C ABI.
+
+The golden checks use the reference's shipped case (tests/golden/): picks must
+equal models/RT_SynMod2D_Inv.rec columns 5 and 7 bit for bit, and the joint
+gradient / misfits must equal what the reference's own code produced.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from helpers import bits_equal, load_fw, load_inv
+
+pytestmark = pytest.mark.gpu
+
+
+def _pg():
+    import pfast_gb300 as pg
+    return pg
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_golden_forward_picks_bit_exact(ctx):
+    """All 56 sources, 33600 traces, 2 reflectors on one GPU; rows of every 4th source
+    checked against the shipped golden columns."""
+    pg, torch = _pg(), _torch()
+    g = load_fw()
+    sv = pg.Survey2D(ctx, 160, 600, float(g["dx"]), float(g["dz"]), g["src"], g["srnum"], g["rec"].astype(np.int32),
+                     numofr=int(g["numofr"]), Z=g["Z"])
+    Tr, st = sv.forward(torch.from_numpy(g["vp"]).cuda())
+    Tr = Tr.cpu().numpy()
+    assert Tr.shape == (33600, 3)
+    assert bits_equal(Tr[g["rows"], 0], g["tt"])
+    assert bits_equal(Tr[g["rows"], 2], g["tr2"])
+    assert st["not_converged"] == 0
+
+
+def test_golden_forward_mixed_within_tolerance(ctx):
+    pg, torch = _pg(), _torch()
+    g = load_fw()
+    sv = pg.Survey2D(ctx, 160, 600, float(g["dx"]), float(g["dz"]), g["src"], g["srnum"], g["rec"].astype(np.int32),
+                     numofr=int(g["numofr"]), Z=g["Z"])
+    Tr, _ = sv.forward(torch.from_numpy(g["vp"]).cuda(), precision=pg.PFAST_MIXED)
+    Tr = Tr.cpu().numpy()
+    assert np.max(np.abs(Tr[g["rows"], 0] - g["tt"]) / g["tt"]) <= 1e-5
+    assert np.max(np.abs(Tr[g["rows"], 2] - g["tr2"]) / g["tr2"]) <= 1e-5
+
+
+def test_golden_joint_gradient_bit_exact(ctx):
+    pg, torch = _pg(), _torch()
+    g = load_inv()
+    Z = load_fw()["Z"]
+    sv = pg.Survey2D(ctx, 160, 600, float(g["dx"]), float(g["dz"]), g["src"], g["srnum"], g["rec"].astype(np.int32),
+                     numofr=int(g["numofr"]), Z=Z, nxy=g["nxy"], tt_obs=g["tt"], tr_obs=g["tr"])
+    WR = torch.full((160, 600), float(g["wr"]), dtype=torch.float64, device="cuda")
+    r = sv.eval(torch.from_numpy(g["vp"]).cuda(), WR)
+    assert float(r["Et"]).hex() == str(g["Et_hex"])
+    assert float(r["Er"]).hex() == str(g["Er_hex"])
+    assert sha(r["gT"].cpu().numpy()) == str(g["gT_sha"])
+    assert sha(r["gR"].cpu().numpy()) == str(g["gR_sha"])
+    assert sha(r["gRT"].cpu().numpy()) == str(g["gRT_sha"])
+    rm = sv.eval(torch.from_numpy(g["vp"]).cuda(), WR, precision=pg.PFAST_MIXED)
+    ref = r["gRT"].cpu().numpy()
+    rel = np.linalg.norm(rm["gRT"].cpu().numpy() - ref) / np.linalg.norm(ref)
+    assert rel <= 1e-4, rel
+
+
+def test_rt_fsm2d_and_adjoint_shims_bit_exact():
+    from oracle import port
+    pg = _pg()
+    g = load_inv()
+    Z = load_fw()["Z"]
+    src, srnum, rec = g["src"], g["srnum"], g["rec"].astype(np.int32)
+    for s in (0, 5):
+        U0, TTd0, TTu0, st, _ = port.rt_fsm2d(g["vp"], Z, src, s, 2, 500, 12.5, 8.0)
+        assert st == 0
+        U, TTd, TTu = np.empty((160, 600)), np.empty((2, 160, 600)), np.empty((2, 160, 600))
+        pg.RT_fsm2d(g["vp"], U, TTd, TTu, Z, src, rec, srnum, s, 2, 500, 12.5, 8.0, 160, 600)
+        assert bits_equal(U, U0) and bits_equal(TTd, TTd0) and bits_equal(TTu, TTu0)
+        LT0, ET0, _ = port.tadjoint2d(U0, g["tt"], rec, g["nxy"], src, srnum, s, 500, 12.5, 8.0)
+        LT = np.empty((160, 600))
+        ET = pg.Tadjoint_fsm2d(LT, U0, g["tt"], rec, g["nxy"], src, srnum, s, 500, 12.5, 8.0, 160, 600)
+        assert bits_equal(LT, LT0) and ET == ET0
+        LR0, ER0, _ = port.radjoint2d(TTu0, g["tr"], rec, g["nxy"], src, srnum, s, 2, 500, 12.5, 8.0)
+        LR = np.empty((160, 600))
+        ER = pg.Radjoint_fsm2d(LR, TTd0, TTu0, g["tr"], rec, g["nxy"], src, srnum, s, 2, 500, 12.5, 8.0, 160, 600)
+        assert bits_equal(LR, LR0) and ER == ER0
+
+
+def test_first_arrival_workload_vs_oracle(ctx):
+    """The 301 x 101 first-arrival workload (21 sources, 301 receivers each, no reflector)."""
+    from oracle import port
+    from pfast_gb300 import synth
+    pg, torch = _pg(), _torch()
+    vp = synth.first_arrival2d_model()
+    src, srnum, rec, nxy = synth.surface_survey2d(101, 301, list(range(0, 301, 15)), list(range(301)))
+    Tr0, st = port.forward2d(vp, None, src, srnum, rec, 0, 500, 10.0, 10.0, nthreads=4)
+    sv = pg.Survey2D(ctx, 101, 301, 10.0, 10.0, src, srnum, rec)
+    Tr, _ = sv.forward(torch.from_numpy(vp).cuda())
+    assert bits_equal(Tr.cpu().numpy(), Tr0)
+
+
+def test_reflection_with_iteration_counter_carry(ctx):
+    """Two reflectors and a small MAXSwp: the reflection adjoint's iteration counter carries over
+    from one reflector to the next, as in the reference."""
+    from oracle import port
+    pg, torch = _pg(), _torch()
+    nr, nc = 50, 120
+    vp = 1600.0 + 25.0 * np.arange(nr)[:, None] + np.zeros((1, nc))
+    Z = np.concatenate([np.stack([np.full(nc, 200.0 + 10 * np.sin(np.arange(nc) / 7.0)), -np.ones(nc),
+                                  np.zeros(nc)], 1),
+                        np.stack([np.full(nc, 420.0), -np.ones(nc), np.zeros(nc)], 1)])
+    src = np.array([[0, 15], [0, 60], [0, 100]], np.int32)
+    rec = np.array([(0, j) for j in range(0, nc, 2)] * 3, np.int32)
+    srnum = np.full(3, nc // 2, np.int32)
+    nxy = np.tile([-1.0, 0.0], (len(rec), 1))
+    Tr, st = port.forward2d(vp, Z, src, srnum, rec, 2, 500, 10.0, 10.0)
+    rng = np.random.default_rng(3)
+    tt = Tr[:, 0] + rng.normal(0, 1e-3, len(rec))
+    tr = Tr[:, 1:] + rng.normal(0, 1e-3, (len(rec), 2))
+    tr[::5, 0] = 0.0
+    WRh = np.full((nr, nc), 0.3)
+    for maxswp in (500, 3):
+        r0 = port.eval2d(vp * 1.02, WRh, Z, src, srnum, rec, nxy, tt, tr, 2, maxswp, 10.0, 10.0)
+        sv = pg.Survey2D(ctx, nr, nc, 10.0, 10.0, src, srnum, rec, numofr=2, Z=Z, nxy=nxy, tt_obs=tt, tr_obs=tr)
+        r = sv.eval(torch.from_numpy(vp * 1.02).cuda(), torch.from_numpy(WRh).cuda(), maxswp=maxswp)
+        assert bits_equal(r["gT"].cpu().numpy(), r0["gT"])
+        assert bits_equal(r["gR"].cpu().numpy(), r0["gR"])
+        assert bits_equal(r["gRT"].cpu().numpy(), r0["gRT"])
+        assert r["Et"] == r0["Et"] and r["Er"] == r0["Er"]
+
+
+def test_reflector_without_node_above_is_an_error(ctx):
+    pg, torch = _pg(), _torch()
+    nr, nc = 20, 30
+    Z = np.stack([np.full(nc, 5.0), -np.ones(nc), np.zeros(nc)], 1)   # above the first row
+    sv = pg.Survey2D(ctx, nr, nc, 10.0, 10.0, np.array([[0, 3]], np.int32), np.array([1], np.int32),
+                     np.array([[0, 5]], np.int32), numofr=1, Z=Z)
+    with pytest.raises(pg.PfastError) as e:
+        sv.forward(torch.full((nr, nc), 2000.0, dtype=torch.float64, device="cuda"))
+    assert e.value.status == 5   # PFAST_ERR_NO_REFLECTION_POINT

@@ -1,0 +1,205 @@
+"""3D parity on the GPU: the CUDA kernels (through the C ABI) against the oracle.
+
+Plain FP64 must be bit-identical (the library is built with -fmad=false, the
+oracle with -ffp-contract=off).  The mixed FP32-bulk + FP64-polish mode must stay
+within the stated tolerances: max relative traveltime error <= 1e-5 and gradient
+relative L2 error <= 1e-4 against the FP64 oracle.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, bits_equal, case3d, picks_from
+
+pytestmark = pytest.mark.gpu
+
+TT_REL_TOL = 1e-5      # mixed mode: max |T - T_oracle| / T_oracle
+GRAD_REL_L2_TOL = 1e-4  # mixed mode: ||g - g_oracle|| / ||g_oracle||
+
+
+def _pg():
+    import pfast_gb300 as pg
+    return pg
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _oracle_case(shape, h, seed):
+    from oracle import port
+    vp, src, srnum, rec, nxyz, noise = case3d(shape, h, seed)
+    Ts = [port.fsm3d(vp, src, s, 100, *h)[0] for s in range(len(srnum))]
+    tobs = picks_from(Ts, src, srnum, rec, noise)
+    return vp, src, srnum, rec, nxyz, tobs, Ts
+
+
+CASES = [((9, 11, 13), (10.0, 10.0, 10.0), 101), ((9, 11, 13), (10.0, 12.5, 8.0), 102),
+         ((17, 19, 23), (20.0, 20.0, 20.0), 103), ((2, 2, 2), (1.0, 1.0, 1.0), 104),
+         ((10, 21, 70), (20.0, 20.0, 20.0), 105), ((5, 3, 33), (5.0, 7.0, 3.0), 106)]
+
+
+@pytest.mark.parametrize("shape,h,seed", CASES)
+def test_fsm3d_shim_bit_exact(shape, h, seed):
+    pg = _pg()
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, seed)
+    for s in range(len(srnum)):
+        U = np.empty(shape)
+        pg.fsm3d(vp, U, src, s, 100, h[0], h[1], h[2], shape[1], shape[2], shape[0])
+        assert bits_equal(U, Ts[s]), (shape, s)
+
+
+@pytest.mark.parametrize("shape,h,seed", CASES)
+def test_adjoint3d_shim_bit_exact(shape, h, seed):
+    from oracle import port
+    pg = _pg()
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, seed)
+    for s in range(len(srnum)):
+        L_ref, E_ref, _ = port.adjoint3d(Ts[s], tobs, rec, nxyz, src, srnum, s, 100, *h)
+        L = np.empty(shape)
+        E = pg.adjoint_fsm3d(L, Ts[s], tobs, rec, nxyz, src, srnum, s, 100, h[0], h[1], h[2], shape[1], shape[2],
+                             shape[0])
+        assert bits_equal(L, L_ref), (shape, s)
+        assert E == E_ref
+
+
+def test_pins_against_reference_hashes(ctx):
+    """The GPU reproduces the fields the reference itself produced (tests/golden/pins3d.json)."""
+    import hashlib
+    pg = _pg()
+    pins = json.load(open(os.path.join(GOLDEN, "pins3d.json")))
+    for c in pins:
+        shape, h = tuple(c["shape"]), c["h"]
+        vp, src, srnum, rec, nxyz, noise = case3d(shape, h, c["seed"])
+        Ts = []
+        for s in range(3):
+            U = np.empty(shape)
+            pg.fsm3d(vp, U, src, s, 100, h[0], h[1], h[2], shape[1], shape[2], shape[0])
+            assert hashlib.sha256(U.tobytes()).hexdigest() == c["sources"][s]["T_sha"]
+            Ts.append(U)
+        tobs = picks_from(Ts, src, srnum, rec, noise)
+        for s in range(3):
+            L = np.empty(shape)
+            E = pg.adjoint_fsm3d(L, Ts[s], tobs, rec, nxyz, src, srnum, s, 100, h[0], h[1], h[2], shape[1],
+                                 shape[2], shape[0])
+            assert hashlib.sha256(L.tobytes()).hexdigest() == c["sources"][s]["L_sha"]
+            assert float(E).hex() == c["sources"][s]["EE_hex"]
+
+
+@pytest.mark.parametrize("shape,h,seed", CASES)
+def test_survey_eval_plain_bit_exact(ctx, shape, h, seed):
+    from oracle import port
+    pg, torch = _pg(), _torch()
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, seed)
+    g_ref, e_ref, fi, ai = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h)
+    sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], h[0], h[1], h[2], src, srnum, rec, nxyz, tobs)
+    g, e, st = sv.eval(torch.from_numpy(vp).cuda())
+    assert bits_equal(g.cpu().numpy(), g_ref)
+    assert e == e_ref
+    assert st["fwd_iters_max"] == int(fi.max())
+    assert st["adj_iters_max"] == int(ai.max())
+    picks, _ = sv.forward(torch.from_numpy(vp).cuda())
+    want = np.concatenate([Ts[s][rec[r, 2], rec[r, 0], rec[r, 1]][None] for s in range(3)
+                           for r in range(sum(srnum[:s]), sum(srnum[:s + 1]))])
+    assert bits_equal(picks.cpu().numpy(), want)
+
+
+def test_batch_split_does_not_change_bits(ctx):
+    pg, torch = _pg(), _torch()
+    shape, h = (10, 21, 70), (20.0, 20.0, 20.0)
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 7)
+    sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src, srnum, rec, nxyz, tobs)
+    d = torch.from_numpy(vp).cuda()
+    g_all, e_all, _ = sv.eval(d)
+    g_one, e_one, st = sv.eval(d, max_batch=1)
+    assert st["batches"] == 3
+    assert bits_equal(g_all.cpu().numpy(), g_one.cpu().numpy()) and e_all == e_one
+
+
+@pytest.mark.parametrize("maxswp", [1, 2])
+def test_iteration_cap_matches_oracle(ctx, maxswp):
+    from oracle import port
+    pg, torch = _pg(), _torch()
+    shape, h = (9, 11, 13), (10.0, 10.0, 10.0)
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 3)
+    g_ref, e_ref, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, maxswp, *h)
+    sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src, srnum, rec, nxyz, tobs)
+    g, e, st = sv.eval(torch.from_numpy(vp).cuda(), maxswp=maxswp)
+    assert bits_equal(g.cpu().numpy(), g_ref) and e == e_ref
+    assert st["not_converged"] > 0
+
+
+def test_edge_receivers_duplicates_unpicked_and_at_source(ctx):
+    """Receivers at the source node, two rows at one node (the later wins), a source with no
+    picked receiver (no adjoint iteration at all) and an empty source."""
+    from oracle import port
+    pg, torch = _pg(), _torch()
+    shape, h = (8, 9, 10), (10.0, 10.0, 10.0)
+    rng = np.random.default_rng(5)
+    vp = 1800.0 + 1000.0 * rng.random(shape)
+    src = np.array([[4, 4, 0], [0, 9, 0], [8, 0, 0], [3, 3, 3]], np.int32)
+    rows = [[(4, 4, 0), (4, 4, 0), (2, 2, 0), (2, 2, 0), (7, 8, 0)],   # at the source, duplicates
+            [(1, 1, 0), (5, 5, 0)],                                      # all unpicked
+            [],                                                          # no receivers
+            [(0, 0, 0), (8, 9, 0), (0, 0, 0)]]
+    srnum = np.array([len(r) for r in rows], np.int32)
+    rec = np.array([x for r in rows for x in r], np.int32)
+    nxyz = np.tile([0.0, 0.0, -1.0], (len(rec), 1))
+    Ts = [port.fsm3d(vp, src, s, 100, *h)[0] for s in range(4)]
+    ch0 = np.concatenate([[0], np.cumsum(srnum)])
+    tobs = np.zeros(len(rec))
+    for s in range(4):
+        for r in range(ch0[s], ch0[s + 1]):
+            tobs[r] = Ts[s][rec[r, 2], rec[r, 0], rec[r, 1]] + 0.003 * (r + 1)
+    tobs[ch0[1]:ch0[2]] = 500.0
+    g_ref, e_ref, _, ai = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h)
+    assert ai[1] == 0 and ai[2] == 0
+    sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src, srnum, rec, nxyz, tobs)
+    g, e, _ = sv.eval(torch.from_numpy(vp).cuda())
+    assert bits_equal(g.cpu().numpy(), g_ref) and e == e_ref
+
+
+def test_host_buffer_entry_matches_device_entry(ctx):
+    pg, torch = _pg(), _torch()
+    shape, h = (17, 19, 23), (20.0, 20.0, 20.0)
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 8)
+    g_h, e_h, _ = pg.eval3d_host(ctx, vp, *h, src, srnum, rec, nxyz, tobs)
+    sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src, srnum, rec, nxyz, tobs)
+    g_d, e_d, _ = sv.eval(torch.from_numpy(vp).cuda())
+    assert bits_equal(g_h, g_d.cpu().numpy()) and e_h == e_d
+
+
+def test_invalid_inputs_raise(ctx):
+    pg = _pg()
+    with pytest.raises(pg.PfastError):
+        pg.Survey3D(ctx, 5, 5, 5, 1.0, 1.0, 1.0, np.array([[5, 0, 0]], np.int32), np.array([0], np.int32),
+                    np.zeros((0, 3), np.int32))
+    with pytest.raises(pg.PfastError):
+        pg.Survey3D(ctx, 5, 1, 5, 1.0, 1.0, 1.0, np.array([[0, 0, 0]], np.int32), np.array([0], np.int32),
+                    np.zeros((0, 3), np.int32))
+
+
+def test_mixed_precision_within_tolerance(ctx):
+    """FP32 bulk + FP64 polish on a smooth heterogeneous model, several tiles per axis."""
+    from oracle import port
+    from pfast_gb300 import synth
+    pg, torch = _pg(), _torch()
+    nz, nr, nc, hh = 24, 40, 72, 20.0
+    vt = synth.true_model3d(nz, nr, nc, hh, seed=4)
+    v0 = synth.gradient_model3d(nz, nr, nc, hh)
+    src, srnum, rec, nxyz = synth.surface_survey3d(nr, nc, 2, 8)
+    tobs = synth.add_noise(port.forward3d(vt, src, srnum, rec, 100, hh, hh, hh, nthreads=4), 0.002, 1)
+    g_ref, e_ref, _, _ = port.eval3d(v0, src, srnum, rec, nxyz, tobs, 100, hh, hh, hh, nthreads=4)
+    sv = pg.Survey3D(ctx, nr, nc, nz, hh, hh, hh, src, srnum, rec, nxyz, tobs)
+    d = torch.from_numpy(v0).cuda()
+    g, e, st = sv.eval(d, precision=pg.PFAST_MIXED)
+    rel = np.linalg.norm(g.cpu().numpy() - g_ref) / np.linalg.norm(g_ref)
+    assert rel <= GRAD_REL_L2_TOL, rel
+    assert abs(e - e_ref) <= 1e-6 * abs(e_ref)
+    picks_ref = port.forward3d(v0, src, srnum, rec, 100, hh, hh, hh, nthreads=4)
+    picks, _ = sv.forward(d, precision=pg.PFAST_MIXED)
+    assert np.max(np.abs(picks.cpu().numpy() - picks_ref) / picks_ref) <= TT_REL_TOL
+    assert st["fwd32_iters_max"] > 0 and st["adj32_iters_max"] > 0

@@ -1,0 +1,150 @@
+"""The oracle restatement (oracle/pfast_oracle.cpp), pinned before it is trusted:
+
+* against the reference's shipped golden picks (models/RT_SynMod2D_Inv.rec
+  columns 5 and 7, committed as tests/golden/rt2d_fw_golden.npz);
+* against gradients / misfits / fields that the reference's own code produced
+  (tests/golden/rt2d_inv_golden.npz, tests/golden/pins3d.json);
+* against the reference built from source here (oracle/_ref), on extra cases,
+  when that build is present.
+CPU only.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import port, ref
+from helpers import GOLDEN, bits_equal, case3d, load_fw, load_inv, picks_from
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_golden_2d_forward_picks_bit_exact():
+    g = load_fw()
+    src, srnum, rec = g["src"], g["srnum"], g["rec"].astype(np.int32)
+    numofr = int(g["numofr"])
+    out = []
+    for s in g["subset"]:
+        Tr, st = port.forward2d(g["vp"], g["Z"], src, srnum, rec, numofr, 500, float(g["dx"]), float(g["dz"]),
+                                s_begin=int(s), s_end=int(s) + 1)
+        assert st == 0
+        out.append(Tr)
+    Tr = np.concatenate(out)
+    assert bits_equal(Tr[:, 0], g["tt"])       # transmission, golden column 5
+    assert bits_equal(Tr[:, 2], g["tr2"])      # second reflector, golden column 7
+
+
+def test_golden_2d_joint_gradient_matches_reference():
+    g = load_inv()
+    n = g["vp"].size
+    r = port.eval2d(g["vp"], np.full(n, float(g["wr"])), load_fw()["Z"], g["src"], g["srnum"], g["rec"].astype(np.int32),
+                    g["nxy"], g["tt"], g["tr"], int(g["numofr"]), 500, float(g["dx"]), float(g["dz"]), nthreads=4)
+    assert r["status"] == 0
+    assert float(r["Et"]).hex() == str(g["Et_hex"])
+    assert float(r["Er"]).hex() == str(g["Er_hex"])
+    assert sha(r["gT"]) == str(g["gT_sha"])
+    assert sha(r["gR"]) == str(g["gR_sha"])
+    assert sha(r["gRT"]) == str(g["gRT_sha"])
+
+
+def test_pins3d_fields_and_misfit_match_reference():
+    pins = json.load(open(os.path.join(GOLDEN, "pins3d.json")))
+    for c in pins:
+        vp, src, srnum, rec, nxyz, noise = case3d(tuple(c["shape"]), c["h"], c["seed"])
+        dx, dy, dz = c["h"]
+        Ts = [port.fsm3d(vp, src, s, 100, dx, dy, dz)[0] for s in range(3)]
+        tobs = picks_from(Ts, src, srnum, rec, noise)
+        for s, want in enumerate(c["sources"]):
+            assert sha(Ts[s]) == want["T_sha"], (c["name"], s)
+            L, E, _ = port.adjoint3d(Ts[s], tobs, rec, nxyz, src, srnum, s, 100, dx, dy, dz)
+            assert sha(L) == want["L_sha"], (c["name"], s)
+            assert float(E).hex() == want["EE_hex"]
+
+
+REF_TREE = os.environ.get("PFAST_REF_ROOT", "/root/reference")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_TREE, "models")), reason="reference tree not present")
+def test_2d_first_iteration_misfit_matches_shipped_log():
+    """par/RT_SynMod2D_Inv_RT.out:142 prints the iteration-1 residuals of the shipped inversion:
+    (TR) 29.0876 ms, (T) 20.6191 ms, (R) 20.5169 ms over all 56 sources and 33600 traces."""
+    from pfast_gb300 import io as pio
+    M = os.path.join(REF_TREE, "models")
+    srcA = pio.readmod(os.path.join(M, "RT_SynMod2D.src"), 168).reshape(56, 3)
+    recA = pio.readmod(os.path.join(M, "RT_SynMod2D_Inv_rand2p.rec"), 33600 * 7).reshape(33600, 7)
+    vp = pio.readmod(os.path.join(M, "RT_SynMod2D_Inv.vp"), 96000).reshape(160, 600)
+    Z = pio.readmod(os.path.join(M, "RT_SynMod2D.ref"), 3600).reshape(1200, 3)
+    src, srnum, rec, nxy, tt, tr = pio.load_survey2d(srcA, recA, 12.5, 8.0, 2)
+    r = port.eval2d(vp, np.full(96000, 0.5), Z, src, srnum, rec, nxy, tt, tr, 2, 500, 12.5, 8.0, nthreads=8)
+    ms = lambda e: 1000 * np.sqrt(2 * e / 33600)
+    assert "%g" % ms(r["Et"] + r["Er"]) == "29.0876"
+    assert "%g" % ms(r["Et"]) == "20.6191"
+    assert "%g" % ms(r["Er"]) == "20.5169"
+
+
+needs_ref = pytest.mark.skipif(not ref.available(), reason="oracle/_ref not built (reference tree absent)")
+
+
+@needs_ref
+@pytest.mark.parametrize("shape,h", [((5, 6, 7), (10.0, 10.0, 10.0)), ((8, 3, 12), (7.0, 11.0, 5.0)),
+                                     ((2, 2, 2), (1.0, 1.0, 1.0)), ((12, 9, 4), (20.0, 20.0, 20.0))])
+def test_oracle_vs_reference_3d(shape, h):
+    vp, src, srnum, rec, nxyz, noise = case3d(shape, h, 7)
+    Ts = []
+    for s in range(3):
+        U, _ = port.fsm3d(vp, src, s, 100, *h)
+        assert bits_equal(U, ref.fsm3d(vp, src, s, 100, *h))
+        Ts.append(U)
+    tobs = picks_from(Ts, src, srnum, rec, noise)
+    # duplicate receiver rows at one node with different picks: the later row wins
+    rec = rec.copy()
+    rec[1] = rec[0]
+    for s in range(3):
+        L, E, _ = port.adjoint3d(Ts[s], tobs, rec, nxyz, src, srnum, s, 100, *h)
+        Lr, Er = ref.adjoint3d(Ts[s], tobs, rec, nxyz, src, srnum, s, 100, *h)
+        assert bits_equal(L, Lr) and E == Er
+
+
+@needs_ref
+def test_oracle_vs_reference_3d_iteration_cap():
+    vp, src, srnum, rec, nxyz, noise = case3d((9, 10, 11), (10.0, 10.0, 10.0), 3)
+    U, it = port.fsm3d(vp, src, 0, 1, 10.0, 10.0, 10.0)   # MAXSwp = 1: stops unconverged
+    assert it == 1
+    assert bits_equal(U, ref.fsm3d(vp, src, 0, 1, 10.0, 10.0, 10.0))
+
+
+@needs_ref
+def test_oracle_vs_reference_2d_synthetic():
+    from pfast_gb300 import synth
+    vt, v0, Zr = synth.joint2d_models(61, 121, 10.0, seed=5)
+    Zr[:, 0] = 380.0 + 30.0 * np.sin(np.arange(121) / 9.0)
+    src, srnum, rec, nxy = synth.surface_survey2d(61, 121, [10, 60, 110], list(range(0, 121, 5)))
+    for s in range(3):
+        a = port.rt_fsm2d(vt, Zr, src, s, 1, 500, 10.0, 10.0)
+        b = ref.rt_fsm2d(vt, Zr, src, s, 1, 500, 10.0, 10.0)
+        assert a[3] == 0
+        for x, y in zip(a[:3], b):
+            assert bits_equal(x, y)
+        rng = np.random.default_rng(s)
+        tt = a[0][rec[:, 0], rec[:, 1]] + rng.normal(0, 1e-3, len(rec))
+        tr = np.stack([a[2][0][rec[:, 0], rec[:, 1]] + rng.normal(0, 1e-3, len(rec))], 1)
+        tr[::7] = 0.0    # unpicked reflections
+        L, E, _ = port.tadjoint2d(a[0], tt, rec, nxy, src, srnum, s, 500, 10.0, 10.0)
+        Lr, Er = ref.tadjoint2d(a[0], tt, rec, nxy, src, srnum, s, 500, 10.0, 10.0)
+        assert bits_equal(L, Lr) and E == Er
+        R, E2, _ = port.radjoint2d(a[2], tr, rec, nxy, src, srnum, s, 1, 500, 10.0, 10.0)
+        Rr, E2r = ref.radjoint2d(a[1], a[2], tr, rec, nxy, src, srnum, s, 1, 500, 10.0, 10.0)
+        assert bits_equal(R, Rr) and E2 == E2r
+
+
+def test_oracle_eval3d_thread_count_invariant():
+    vp, src, srnum, rec, nxyz, noise = case3d((7, 8, 9), (10.0, 10.0, 10.0), 11)
+    Ts = [port.fsm3d(vp, src, s, 100, 10.0, 10.0, 10.0)[0] for s in range(3)]
+    tobs = picks_from(Ts, src, srnum, rec, noise)
+    g1, e1, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, 10.0, 10.0, 10.0, nthreads=1)
+    g3, e3, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, 10.0, 10.0, 10.0, nthreads=3)
+    assert bits_equal(g1, g3) and e1 == e3
