@@ -477,12 +477,13 @@ void adjoint2d_sweeps(double* L, const double* T, const unsigned char* fixed, co
 
 // Receiver BC for one 2D field (the bodies of src/RT_padjoint2d.h:311-339 and 405-433).
 // trans=true: transmission (pick if obs<100, no BC at the source node);
-// trans=false: reflection (pick if obs!=0, BC everywhere).
-double receiver_bc2d(double* L, const double* T, const double* obs, int obs_stride, int obs_off,
-                     const int* rec, const double* nxy, int si, int sj, int ch0, int nrec,
-                     const Grid2& g, double dx, double dz, unsigned char* fixed, bool trans) {
+// trans=false: reflection (pick if obs!=0, BC everywhere).  The misfit terms are
+// added to E in row order; the reflection adjoint keeps one running sum over all
+// its reflectors (src/RT_padjoint2d.h:409).
+void receiver_bc2d(double* L, const double* T, const double* obs, int obs_stride, int obs_off,
+                   const int* rec, const double* nxy, int si, int sj, int ch0, int nrec,
+                   const Grid2& g, double dx, double dz, unsigned char* fixed, bool trans, double& E) {
     const double Cr = 1.0;
-    double E = 0.0;
     for (int r = 0; r < nrec; ++r) {
         const int row = ch0 + r;
         const double tob = obs[(int64_t)row * obs_stride + obs_off];
@@ -500,7 +501,6 @@ double receiver_bc2d(double* L, const double* T, const double* obs, int obs_stri
         else
             L[o] = 0.0;
     }
-    return E;
 }
 
 } // namespace
@@ -517,8 +517,9 @@ double oracle_tadjoint2d(double* L, const double* T, const double* Tobs, const i
     for (int s = 0; s < srcid; ++s) ch0 += srnum[s];
     std::vector<unsigned char> fixed(n, 0);
     for (int64_t t = 0; t < n; ++t) L[t] = 0.0;
-    double E = receiver_bc2d(L, T, Tobs, 1, 0, rec, nxy, src[srcid * 2], src[srcid * 2 + 1], ch0,
-                             srnum[srcid], g, dx, dz, fixed.data(), true);
+    double E = 0.0;
+    receiver_bc2d(L, T, Tobs, 1, 0, rec, nxy, src[srcid * 2], src[srcid * 2 + 1], ch0, srnum[srcid], g, dx, dz,
+                  fixed.data(), true, E);
     int count = 0;
     adjoint2d_sweeps(L, T, fixed.data(), g, maxswp, dx, dz, count, iters);
     return E;
@@ -543,8 +544,8 @@ double oracle_radjoint2d(double* UR, const double* Tu, const double* TRobs, cons
     for (int ir = 0; ir < numofr; ++ir) {
         for (int64_t t = 0; t < n; ++t) L[t] = 0.0;
         const double* T = Tu + (int64_t)ir * n;
-        E += receiver_bc2d(L.data(), T, TRobs, numofr, ir, rec, nxy, src[srcid * 2], src[srcid * 2 + 1],
-                           ch0, srnum[srcid], g, dx, dz, fixed.data(), false);
+        receiver_bc2d(L.data(), T, TRobs, numofr, ir, rec, nxy, src[srcid * 2], src[srcid * 2 + 1], ch0,
+                      srnum[srcid], g, dx, dz, fixed.data(), false, E);
         adjoint2d_sweeps(L.data(), T, fixed.data(), g, maxswp, dx, dz, count, iters ? iters + ir : nullptr);
         for (int64_t t = 0; t < n; ++t) UR[t] = UR[t] + L[t];
     }

@@ -10,6 +10,6 @@ from ._capi import lib as _lib
 _lib()  # fail loudly when the CUDA library is missing
 
 from .api import *  # noqa: E402,F401,F403
-from . import api, synth, io  # noqa: E402,F401
+from . import api, synth, io, workloads  # noqa: E402,F401
 
 __version__ = "0.1.0"

@@ -159,8 +159,7 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
             a.first = dir == 0;
             a.last = dir == 7;
             for (int d = 0; d < dt.ndiag; ++d) {
-                PFAST_TRY(launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
-                ++ctx->launches;
+                PFAST_LAUNCH(ctx, launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
             }
         }
         cudaError_t le = cudaGetLastError();
@@ -213,7 +212,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     int* nc_ptr = st ? &st->not_converged : &dummy_nc;
     long long* nu = st ? &st->fwd_node_updates : nullptr;
     if (precision == PFAST_PLAIN_FP64) {
-        PFAST_TRY(launch_init_fwd3(ctx->T64.p, 0, N, N, src_lin, nb, s));
+        PFAST_LAUNCH(ctx, launch_init_fwd3(ctx->T64.p, 0, N, N, src_lin, nb, s));
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = ctx->T64.p;
         a.snap = ctx->scratch.p;
@@ -230,7 +229,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     } else {
         float* T32 = ctx->scratch.as<float>();
         float* snap32 = T32 + N * nb;
-        PFAST_TRY(launch_init_fwd3(T32, 1, N, N, src_lin, nb, s));
+        PFAST_LAUNCH(ctx, launch_init_fwd3(T32, 1, N, N, src_lin, nb, s));
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = T32;
         a.snap = snap32;
@@ -240,7 +239,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         PFAST_TRY(run_sweeps3(ctx, a, kFwdFast32, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
                               st ? &st->ms_fwd32 : nullptr));
         if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
-        PFAST_TRY(launch_widen(T32, ctx->T64.as<double>(), N, N, N, nb, s));
+        PFAST_LAUNCH(ctx, launch_widen(T32, ctx->T64.as<double>(), N, N, N, nb, s));
         std::fill(iters.begin(), iters.end(), 0);
         active.resize(nb);
         for (int b = 0; b < nb; ++b) active[b] = b;
@@ -300,7 +299,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     bc.dx = sv->dx;
     bc.dy = sv->dy;
     bc.dz = sv->dz;
-    PFAST_TRY(launch_bc3(bc, nb, s));
+    PFAST_LAUNCH(ctx, launch_bc3(bc, nb, s));
     PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->h_ee.p, ctx->ee.p, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
     PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->h_need.p, ctx->need.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, s));
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
@@ -336,7 +335,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         std::vector<int> active64 = active;
         float* L32 = ctx->scratch.as<float>();
         float* snap32 = L32 + N * nb;
-        PFAST_TRY(launch_narrow(ctx->L64.as<double>(), L32, N, N, N, nb, s));
+        PFAST_LAUNCH(ctx, launch_narrow(ctx->L64.as<double>(), L32, N, N, N, nb, s));
         a.field = L32;
         a.snap = snap32;
         a.tol_abs = kTol32AbsAdj;
@@ -344,7 +343,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         PFAST_TRY(run_sweeps3(ctx, a, kAdjFast32, *dt, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
                               st ? &st->ms_adj32 : nullptr));
         if (st) for (int v : iters) st->adj32_iters_max = std::max(st->adj32_iters_max, v);
-        PFAST_TRY(launch_widen_lambda(L32, ctx->L64.as<double>(), ctx->mask.as<unsigned>(), N, N, mwords, sv->nz,
+        PFAST_LAUNCH(ctx, launch_widen_lambda(L32, ctx->L64.as<double>(), ctx->mask.as<unsigned>(), N, N, mwords, sv->nz,
                                       sv->nr, sv->nc, wpr, nb, s));
         std::fill(iters.begin(), iters.end(), 0);
         a.field = ctx->L64.p;
@@ -596,7 +595,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     const long long launches0 = ctx->launches;
     PFAST_TRY(ctx->s64.ensure(sizeof(double) * N));
     PFAST_TRY(ctx->s32.ensure(sizeof(float) * N));
-    PFAST_TRY(launch_slowness(vp, ctx->s64.as<double>(), o.precision == PFAST_MIXED ? ctx->s32.as<float>() : nullptr, N, s));
+    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), o.precision == PFAST_MIXED ? ctx->s32.as<float>() : nullptr, N, s));
     if (want_grad) PFAST_CUDA_TRY(cudaMemsetAsync(grad, 0, sizeof(double) * N, s));
     const size_t per_src = (size_t)N * (want_grad ? 24 : 16) + (size_t)sv->nz * sv->nr * ((sv->nc + 31) / 32) * 4;
     const int B = pick_batch(std::max(sv->nsrc, 1), o.max_batch, per_src);
@@ -609,9 +608,9 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
         if (want_grad) {
             PFAST_TRY(adjoint3d_batch(ctx, sv, b0, nb, o.precision, o.maxswp, ee.data(), stats));
             for (int b = 0; b < nb; ++b) E += ee[b];   // loc_E += EE in source order
-            PFAST_TRY(launch_accumulate(grad, ctx->L64.as<double>(), N, vp, N, nb, s));
+            PFAST_LAUNCH(ctx, launch_accumulate(grad, ctx->L64.as<double>(), N, vp, N, nb, s));
         }
-        if (picks) PFAST_TRY(launch_gather3(ctx->T64.as<double>(), N, sv->d_rec, sv->d_ch0 + b0, sv->d_srnum + b0, nb,
+        if (picks) PFAST_LAUNCH(ctx, launch_gather3(ctx->T64.as<double>(), N, sv->d_rec, sv->d_ch0 + b0, sv->d_srnum + b0, nb,
                                             sv->nz, sv->nr, sv->nc, picks, s));
     }
     PFAST_CUDA_TRY(cudaEventRecord(t1, s));

@@ -90,6 +90,14 @@ struct pfast_survey2d {
     int geom_status = 0;             // PFAST_ERR_NO_REFLECTION_POINT if a reflector has no node above it
 };
 
+// Launch a kernel through one of the launch_* helpers and count it in ctx->launches.
+#define PFAST_LAUNCH(ctx, expr)                \
+    do {                                        \
+        pfast_status s__ = (expr);              \
+        if (s__ != PFAST_OK) return s__;        \
+        ++(ctx)->launches;                      \
+    } while (0)
+
 namespace pfast {
 
 pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, DiagTable3** out);

@@ -111,8 +111,7 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
             a.first = dir == 0;
             a.last = dir == 3;
             for (int d = 0; d < dt.ndiag; ++d) {
-                PFAST_TRY2(launch_sweep2(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
-                ++ctx->launches;
+                PFAST_LAUNCH(ctx, launch_sweep2(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
             }
         }
         cudaError_t le = cudaGetLastError();
@@ -176,7 +175,7 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
     int* ncv = st ? &st->not_converged : &dummy;
     long long* nu = st ? &st->fwd_node_updates : nullptr;
     if (precision == PFAST_PLAIN_FP64) {
-        if (init) PFAST_TRY2(launch_init2(fields, 0, d.off, d.srcnode, N, ninst, s));
+        if (init) PFAST_LAUNCH(ctx, launch_init2(fields, 0, d.off, d.srcnode, N, ninst, s));
         a.field = fields;
         a.inst_off = d.off;
         a.aux = s64;
@@ -192,8 +191,8 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
     } else {
         float* f32 = ctx->scratch.as<float>();
         float* snap32 = f32 + N * ninst;
-        if (init) PFAST_TRY2(launch_init2(f32, 1, d.off32, d.srcnode, N, ninst, s));
-        else PFAST_TRY2(launch_narrow_inst(fields, f32, d.off, d.off32, N, ninst, s));
+        if (init) PFAST_LAUNCH(ctx, launch_init2(f32, 1, d.off32, d.srcnode, N, ninst, s));
+        else PFAST_LAUNCH(ctx, launch_narrow_inst(fields, f32, d.off, d.off32, N, ninst, s));
         a.field = f32;
         a.inst_off = d.off32;
         a.aux = s32;
@@ -202,7 +201,7 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
         PFAST_TRY2(run_sweeps2(ctx, a, kFwdFast32, *dt, ninst, active, caps, iters.data(), N, nu, ncv,
                                st ? &st->ms_fwd32 : nullptr));
         if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
-        PFAST_TRY2(launch_widen_inst(f32, fields, d.off32, d.off, N, ninst, s));
+        PFAST_LAUNCH(ctx, launch_widen_inst(f32, fields, d.off32, d.off, N, ninst, s));
         active.resize(ninst);
         for (int q = 0; q < ninst; ++q) { active[q] = q; iters[q] = 0; }
         a.field = fields;
@@ -259,7 +258,7 @@ pfast_status forward2d_batch(pfast_ctx* ctx, pfast_survey2d* sv, int b0, int nb,
     PFAST_TRY2(upload_inst(ctx, ctx->misc, B, bd));
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
     const int nB = (int)B.off.size();
-    PFAST_TRY2(launch_copy_inst(F, F, 0, bd.aux_off, bd.off, N, nB, s));
+    PFAST_LAUNCH(ctx, launch_copy_inst(F, F, 0, bd.aux_off, bd.off, N, nB, s));
     PFAST_TRY2(ctx->need.ensure(sizeof(int)));
     PFAST_CUDA_TRY(cudaMemsetAsync(ctx->need.p, 0, sizeof(int), s));
     Reflect2Args ra;
@@ -275,7 +274,7 @@ pfast_status forward2d_batch(pfast_ctx* ctx, pfast_survey2d* sv, int b0, int nb,
     ra.dx = sv->dx;
     ra.dz = sv->dz;
     ra.err = ctx->need.as<int>();
-    PFAST_TRY2(launch_reflect2(ra, nB, s));
+    PFAST_LAUNCH(ctx, launch_reflect2(ra, nB, s));
     int herr = 0;
     PFAST_CUDA_TRY(cudaMemcpyAsync(&herr, ctx->need.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
@@ -344,7 +343,7 @@ pfast_status adj_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* L, const dou
     bc.nc = sv->nc;
     bc.dx = sv->dx;
     bc.dz = sv->dz;
-    PFAST_TRY2(launch_bc2(bc, ninst, s));
+    PFAST_LAUNCH(ctx, launch_bc2(bc, ninst, s));
     PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->h_need.p, ctx->need.p, sizeof(int) * ninst, cudaMemcpyDeviceToHost, s));
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
     PFAST_CUDA_TRY(cudaStreamSynchronize(s));
@@ -382,7 +381,7 @@ pfast_status adj_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* L, const dou
         std::vector<int> it32(ninst, 0);
         float* f32 = ctx->scratch.as<float>();
         float* snap32 = f32 + N * ninst;
-        PFAST_TRY2(launch_narrow_inst(L, f32, d.off, d.off32, N, ninst, s));
+        PFAST_LAUNCH(ctx, launch_narrow_inst(L, f32, d.off, d.off32, N, ninst, s));
         a.field = f32;
         a.inst_off = d.off32;
         a.snap = snap32;
@@ -391,7 +390,7 @@ pfast_status adj_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* L, const dou
         PFAST_TRY2(run_sweeps2(ctx, a, kAdjFast32, *dt, ninst, active, caps, it32.data(), interior, nu, ncv,
                                st ? &st->ms_adj32 : nullptr));
         if (st) for (int v : it32) st->adj32_iters_max = std::max(st->adj32_iters_max, v);
-        PFAST_TRY2(launch_widen_lambda_inst(f32, L, d.off32, d.off, ctx->mask.as<unsigned>(), d.mask_off, sv->nr,
+        PFAST_LAUNCH(ctx, launch_widen_lambda_inst(f32, L, d.off32, d.off, ctx->mask.as<unsigned>(), d.mask_off, sv->nr,
                                             sv->nc, (sv->nc + 31) / 32, ninst, s));
         a.field = L;
         a.inst_off = d.off;
@@ -468,7 +467,7 @@ pfast_status adjoint2d_batch(pfast_ctx* ctx, pfast_survey2d* sv, int b0, int nb,
         add.aux_off = sof;
         InstDev ad;
         PFAST_TRY2(upload_inst(ctx, ctx->misc, add, ad));
-        PFAST_TRY2(launch_addto2(LB, ad.off, LC, ad.aux_off, N, nb, s));
+        PFAST_LAUNCH(ctx, launch_addto2(LB, ad.off, LC, ad.aux_off, N, nb, s));
     }
     PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->h_ee.p, ctx->ee.p, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, s));
     PFAST_CUDA_TRY(cudaStreamSynchronize(s));
@@ -511,7 +510,7 @@ pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp
     const long long l0 = ctx->launches;
     PFAST_TRY2(ctx->s64.ensure(sizeof(double) * N));
     PFAST_TRY2(ctx->s32.ensure(sizeof(float) * N));
-    PFAST_TRY2(launch_slowness(vp, ctx->s64.as<double>(), ctx->s32.as<float>(), N, s));
+    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), ctx->s32.as<float>(), N, s));
     const size_t per_src = (size_t)N * 8 * (1 + 2 * R) + (size_t)N * 16 * (1 + R);
     const int B = pick_batch2(std::max(sv->nsrc, 1), (TTd_host || TT_host) ? 1 : o.max_batch, per_src);
     for (int b0 = 0; b0 < sv->nsrc; b0 += B) {
@@ -525,7 +524,7 @@ pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp
             t.off = sfo;
             InstDev d;
             PFAST_TRY2(upload_inst(ctx, ctx->misc, t, d));
-            PFAST_TRY2(launch_gather2(ctx->f2a.as<double>(), d.off, R, N, sv->d_rec, sv->d_ch0, sv->d_srnum, nb, b0,
+            PFAST_LAUNCH(ctx, launch_gather2(ctx->f2a.as<double>(), d.off, R, N, sv->d_rec, sv->d_ch0, sv->d_srnum, nb, b0,
                                       sv->nc, Tr, s));
         }
         if (TT_host) {   // single-source shim path (B == 1)
@@ -565,7 +564,7 @@ pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, c
     const long long l0 = ctx->launches;
     PFAST_TRY2(ctx->s64.ensure(sizeof(double) * N));
     PFAST_TRY2(ctx->s32.ensure(sizeof(float) * N));
-    PFAST_TRY2(launch_slowness(vp, ctx->s64.as<double>(), ctx->s32.as<float>(), N, s));
+    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), ctx->s32.as<float>(), N, s));
     PFAST_CUDA_TRY(cudaMemsetAsync(gT, 0, sizeof(double) * N, s));
     PFAST_CUDA_TRY(cudaMemsetAsync(gR, 0, sizeof(double) * N, s));
     const size_t per_src = (size_t)N * 8 * (1 + 2 * R + 3) + (size_t)N * 16 * (1 + R);
@@ -590,9 +589,9 @@ pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, c
         acc.lim = slot;
         InstDev d;
         PFAST_TRY2(upload_inst(ctx, ctx->misc, acc, d));
-        PFAST_TRY2(launch_accumulate2(gT, gR, ctx->f2b.as<double>(), d.off, d.lim, vp, N, 2 * nb, s));
+        PFAST_LAUNCH(ctx, launch_accumulate2(gT, gR, ctx->f2b.as<double>(), d.off, d.lim, vp, N, 2 * nb, s));
     }
-    PFAST_TRY2(launch_blend2(gT, gR, WR, gRT, N, s));
+    PFAST_LAUNCH(ctx, launch_blend2(gT, gR, WR, gRT, N, s));
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[7], s));
     PFAST_CUDA_TRY(cudaStreamSynchronize(s));
     if (st) {

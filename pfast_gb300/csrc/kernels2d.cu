@@ -80,17 +80,47 @@ __device__ __forceinline__ double adj2_plain(double T0, double Txp, double Txm, 
     return 0.0;
 }
 
+// Fast adjoint forms (see kernels3d.cu): den = sum_m w_m max(-e_m, 0),
+// num = sum_m w_m max(e_m, 0) lambda_m with e_m = T_m - T0.
 template <typename R>
-__device__ __forceinline__ R adj2_fast(R T0, R Txp, R Txm, R Tzp, R Tzm, R Lxp, R Lxm, R Lzp, R Lzm, R rdx, R rdz,
-                                       R tinf) {
-    if (Txp >= tinf || T0 >= tinf || Txm >= tinf || Tzp >= tinf || Tzm >= tinf) return R(0);
-    const R gxp = (T0 - Txp) * rdx, gxm = (Txm - T0) * rdx;
-    const R gzp = (T0 - Tzp) * rdz, gzm = (Tzm - T0) * rdz;
+__device__ __forceinline__ void adj2_terms(R T0, R Txp, R Txm, R Tzp, R Tzm, R Lxp, R Lxm, R Lzp, R Lzm, R wx, R wz,
+                                           R& num, R& den) {
     const R z = R(0);
-    const R den = (fmax(gxp, z) - fmin(gxm, z)) * rdx + (fmax(gzp, z) - fmin(gzm, z)) * rdz;
-    if (!(fabs(den) > R(1e-9))) return z;
-    const R num = (fmax(gxm, z) * Lxm - fmin(gxp, z) * Lxp) * rdx + (fmax(gzm, z) * Lzm - fmin(gzp, z) * Lzp) * rdz;
-    return num / den;
+    R e;
+    e = Txp - T0; den = wx * fmax(-e, z); num = wx * fmax(e, z) * Lxp;
+    e = Txm - T0; den = fma(wx, fmax(-e, z), den); num = fma(wx * fmax(e, z), Lxm, num);
+    e = Tzp - T0; den = fma(wz, fmax(-e, z), den); num = fma(wz * fmax(e, z), Lzp, num);
+    e = Tzm - T0; den = fma(wz, fmax(-e, z), den); num = fma(wz * fmax(e, z), Lzm, num);
+}
+
+__device__ __forceinline__ float adj2_bulk(float T0, float Txp, float Txm, float Tzp, float Tzm, float Lxp, float Lxm,
+                                           float Lzp, float Lzm, float wx, float wz) {
+    const float ti = INFINITY;
+    if (Txp >= ti || T0 >= ti || Txm >= ti || Tzp >= ti || Tzm >= ti) return 0.f;
+    float num, den;
+    adj2_terms<float>(T0, Txp, Txm, Tzp, Tzm, Lxp, Lxm, Lzp, Lzm, wx, wz, num, den);
+    return (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
+}
+
+__device__ __forceinline__ double adj2_polish(double T0, double Txp, double Txm, double Tzp, double Tzm, double Lxp,
+                                              double Lxm, double Lzp, double Lzm, double L0, double wx, double wz) {
+    if (Txp >= kInf || T0 >= kInf || Txm >= kInf || Tzp >= kInf || Tzm >= kInf) return 0.0;
+    double num, den;
+    adj2_terms<double>(T0, Txp, Txm, Tzp, Tzm, Lxp, Lxm, Lzp, Lzm, wx, wz, num, den);
+    if (!(fabs(den) > 1e-9)) return 0.0;
+    const double r = fma(-den, L0, num);
+    return L0 + (double)__fdividef((float)r, (float)den);
+}
+
+// FP64 polish Godunov update, one Newton step on f(q) = wx max(q-a,0)^2 + wz max(q-b,0)^2 - s^2
+// (FP64 residual, FP32 step); a: x-neighbour minimum, b: z-neighbour minimum.
+__device__ __forceinline__ double eik2_newton(double U0, double a, double b, double s, double dx, double dz, double wx,
+                                              double wz) {
+    const double px = fmax(U0 - a, 0.0), pz = fmax(U0 - b, 0.0);
+    const double f = fma(wx * px, px, fma(wz * pz, pz, -s * s));
+    const float fp = 2.0f * ((float)wx * (float)px + (float)wz * (float)pz);
+    if (!(fp > 0.0f)) return fmin(fma(dx, s, a), fma(dz, s, b));
+    return U0 - (double)__fdividef((float)f, fp);
 }
 
 template <typename Dst, typename Src, typename Conv>
@@ -192,9 +222,8 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     const Aux* slow = reinterpret_cast<const Aux*>(A.aux);
     const bool row_interior = gi >= 1 && gi <= nr - 2;
 
-    const Real rdx = Real(1.0 / A.dx), rdz = Real(1.0 / A.dz);
-    const Real wx = Real(A.inv2x), wz = Real(A.inv2z);
-    const Real rsum = Real(1.0 / (A.inv2x + A.inv2z));
+    const float wx = float(A.inv2x), wz = float(A.inv2z);
+    const float rsum = float(1.0 / (A.inv2x + A.inv2z));
     const int cb = (li + 1) * R2 + 1;
     const int steps = ei + ej - 1;
 
@@ -218,8 +247,7 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         const float qv = eik2_fast<float>(ax, bz, s, (float)A.dx, (float)A.dz, wx, wz, rsum);
                         box[c] = ref_min(box[c], qv);
                     } else {
-                        const double qv = eik2_fast<double>(ax, bz, s, A.dx, A.dz, wx, wz, rsum);
-                        if (qv < kInf) box[c] = qv;
+                        box[c] = eik2_newton(box[c], ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z);
                     }
                 }
             } else {
@@ -229,10 +257,12 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                     if constexpr (KIND == kAdjPlain64) {
                         r = adj2_plain(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
                                        box[c - 1], box[c + R2], box[c - R2], A.dx, A.dz);
+                    } else if constexpr (KIND == kAdjFast32) {
+                        r = adj2_bulk(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
+                                      box[c - 1], box[c + R2], box[c - R2], (float)A.inv2x, (float)A.inv2z);
                     } else {
-                        const Real tinf = (KIND == kAdjFast32) ? Real(INFINITY) : Real(kInf);
-                        r = adj2_fast<Real>(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
-                                            box[c - 1], box[c + R2], box[c - R2], rdx, rdz, tinf);
+                        r = adj2_polish(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
+                                        box[c - 1], box[c + R2], box[c - R2], box[c], A.inv2x, A.inv2z);
                     }
                     box[c] = r;
                 }

@@ -144,24 +144,65 @@ __device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, 
     return 0.0;
 }
 
-// Fast adjoint update: the same upwind formula with reciprocal multiplies.  T
-// values may be offsets from a common reference (differences are unchanged);
-// an unreached neighbour is marked by T >= tinf.
+// Fast adjoint update.  The reference's upwind formula (src/T_padjoint3d.h:51-66)
+// collapses, with w = 1/d^2 of each neighbour's axis and e_m = T_m - T0, to
+//   den = sum_m w_m max(-e_m, 0),   num = sum_m w_m max(e_m, 0) lambda_m,   lambda = num / den
+// (POS(-(T_p-T0)/d) = max(-e_p,0)/d, -NEG(-(T0-T_m)/d) = max(-e_m,0)/d, and so on).
+// T values may be offsets from a common reference; an unreached node has T >= tinf.
 template <typename R>
-__device__ __forceinline__ R adj3_fast(R T0, R Txp, R Txm, R Typ, R Tym, R Tzp, R Tzm, R Lxp, R Lxm, R Lyp,
-                                       R Lym, R Lzp, R Lzm, R rdx, R rdy, R rdz, R tinf) {
-    if (T0 >= tinf || Txp >= tinf || Txm >= tinf || Typ >= tinf || Tym >= tinf || Tzp >= tinf || Tzm >= tinf)
-        return R(0);
-    const R gxp = (T0 - Txp) * rdx, gxm = (Txm - T0) * rdx;
-    const R gyp = (T0 - Typ) * rdy, gym = (Tym - T0) * rdy;
-    const R gzp = (T0 - Tzp) * rdz, gzm = (Tzm - T0) * rdz;
+__device__ __forceinline__ void adj3_terms(R T0, R Txp, R Txm, R Typ, R Tym, R Tzp, R Tzm, R Lxp, R Lxm, R Lyp,
+                                           R Lym, R Lzp, R Lzm, R wx, R wy, R wz, R& num, R& den) {
     const R z = R(0);
-    const R den = (fmax(gxp, z) - fmin(gxm, z)) * rdx + (fmax(gyp, z) - fmin(gym, z)) * rdy +
-                  (fmax(gzp, z) - fmin(gzm, z)) * rdz;
-    if (!(fabs(den) > R(1e-9))) return z;
-    const R num = (fmax(gxm, z) * Lxm - fmin(gxp, z) * Lxp) * rdx + (fmax(gym, z) * Lym - fmin(gyp, z) * Lyp) * rdy +
-                  (fmax(gzm, z) * Lzm - fmin(gzp, z) * Lzp) * rdz;
-    return num / den;
+    R e;
+    e = Txp - T0; den = wx * fmax(-e, z); num = wx * fmax(e, z) * Lxp;
+    e = Txm - T0; den = fma(wx, fmax(-e, z), den); num = fma(wx * fmax(e, z), Lxm, num);
+    e = Typ - T0; den = fma(wy, fmax(-e, z), den); num = fma(wy * fmax(e, z), Lyp, num);
+    e = Tym - T0; den = fma(wy, fmax(-e, z), den); num = fma(wy * fmax(e, z), Lym, num);
+    e = Tzp - T0; den = fma(wz, fmax(-e, z), den); num = fma(wz * fmax(e, z), Lzp, num);
+    e = Tzm - T0; den = fma(wz, fmax(-e, z), den); num = fma(wz * fmax(e, z), Lzm, num);
+}
+
+template <typename R>
+__device__ __forceinline__ bool any_unreached(R T0, R a, R b, R c, R d, R e, R f, R tinf) {
+    return T0 >= tinf || a >= tinf || b >= tinf || c >= tinf || d >= tinf || e >= tinf || f >= tinf;
+}
+
+// FP32 bulk adjoint update.
+__device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float Typ, float Tym, float Tzp, float Tzm,
+                                           float Lxp, float Lxm, float Lyp, float Lym, float Lzp, float Lzm, float wx,
+                                           float wy, float wz) {
+    if (any_unreached(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, INFINITY)) return 0.f;
+    float num, den;
+    adj3_terms<float>(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, wx, wy, wz, num, den);
+    return (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
+}
+
+// FP64 polish adjoint update in residual-correction form: the residual
+// r = num - den*lambda0 is formed in FP64, the correction r/den in FP32.
+__device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm, double Typ, double Tym, double Tzp,
+                                              double Tzm, double Lxp, double Lxm, double Lyp, double Lym, double Lzp,
+                                              double Lzm, double L0, double wx, double wy, double wz) {
+    if (any_unreached(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, kInf)) return 0.0;
+    double num, den;
+    adj3_terms<double>(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, wx, wy, wz, num, den);
+    if (!(fabs(den) > 1e-9)) return 0.0;
+    const double r = fma(-den, L0, num);
+    return L0 + (double)__fdividef((float)r, (float)den);
+}
+
+// FP64 polish Godunov update in residual-correction form: one Newton step from the
+// current value U0 on f(q) = sum_m w_m max(q - a_m, 0)^2 - s^2, whose root is the
+// Godunov value (the 1-, 2- and 3-term cases of src/T_pfsm3d.h:106-118 are the
+// pieces of this function).  f is evaluated in FP64, the step f / f' in FP32.
+__device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s, const Spacing3& sp) {
+    const double px = fmax(U0 - a, 0.0), py = fmax(U0 - b, 0.0), pz = fmax(U0 - c, 0.0);
+    const double wx = sp.inv2[0], wy = sp.inv2[1], wz = sp.inv2[2];
+    const double f = fma(wx * px, px, fma(wy * py, py, fma(wz * pz, pz, -s * s)));
+    const float fp = 2.0f * ((float)wx * (float)px + (float)wy * (float)py + (float)wz * (float)pz);
+    if (!(fp > 0.0f)) {   // U0 at or below every neighbour: restart from the 1-term value
+        return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
+    }
+    return U0 - (double)__fdividef((float)f, fp);
 }
 
 // ----------------------------------------------------------- tile I/O
@@ -294,9 +335,9 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     if constexpr (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
     const bool row_interior = ADJ ? (gk >= 1 && gk <= nz - 2 && gi >= 1 && gi <= nr - 2) : true;
 
-    FastConst<Real> K;
-    if constexpr (KIND == kFwdFast32 || KIND == kFwdPolish64) K = fast_const<Real>(A.sp);
-    const Real rdx = Real(1.0 / A.sp.d[0]), rdy = Real(1.0 / A.sp.d[1]), rdz = Real(1.0 / A.sp.d[2]);
+    FastConst<float> K;
+    if constexpr (KIND == kFwdFast32) K = fast_const<float>(A.sp);
+    const float wx32 = (float)A.sp.inv2[0], wy32 = (float)A.sp.inv2[1], wz32 = (float)A.sp.inv2[2];
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
@@ -317,9 +358,8 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                     } else if constexpr (KIND == kFwdFast32) {
                         const float q = eik3_fast<float>(xa, yb, zc, s, K);
                         box[c] = ref_min(box[c], q);
-                    } else {   // polish: the Godunov value itself, unless unreachable
-                        const double q = eik3_fast<double>(xa, yb, zc, s, K);
-                        if (q < kInf) box[c] = q;
+                    } else {   // polish: one Newton step of the local Godunov equation
+                        box[c] = eik3_newton(box[c], xa, yb, zc, s, A.sp);
                     }
                 }
             } else {
@@ -329,11 +369,14 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                         r = adj3_plain(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
                                        aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
                                        box[c - PS], A.sp);
+                    } else if constexpr (KIND == kAdjFast32) {
+                        r = adj3_bulk(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                      aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
+                                      box[c - PS], wx32, wy32, wz32);
                     } else {
-                        const Real tinf = (KIND == kAdjFast32) ? Real(INFINITY) : Real(kInf);
-                        r = adj3_fast<Real>(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                            aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ],
-                                            box[c + PS], box[c - PS], rdx, rdy, rdz, tinf);
+                        r = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                        aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
+                                        box[c - PS], box[c], A.sp.inv2[0], A.sp.inv2[1], A.sp.inv2[2]);
                     }
                     box[c] = r;
                 }

@@ -118,26 +118,32 @@ def test_oracle_vs_reference_3d_iteration_cap():
 
 
 @needs_ref
-def test_oracle_vs_reference_2d_synthetic():
+@pytest.mark.parametrize("maxswp", [500, 3])
+def test_oracle_vs_reference_2d_synthetic(maxswp):
+    """Two reflectors, both picked: the reflection misfit is one running sum over the
+    reflectors and the iteration counter carries from one reflector to the next."""
     from pfast_gb300 import synth
     vt, v0, Zr = synth.joint2d_models(61, 121, 10.0, seed=5)
     Zr[:, 0] = 380.0 + 30.0 * np.sin(np.arange(121) / 9.0)
+    Z2 = Zr.copy()
+    Z2[:, 0] = 520.0
+    Z = np.concatenate([Zr, Z2])
     src, srnum, rec, nxy = synth.surface_survey2d(61, 121, [10, 60, 110], list(range(0, 121, 5)))
     for s in range(3):
-        a = port.rt_fsm2d(vt, Zr, src, s, 1, 500, 10.0, 10.0)
-        b = ref.rt_fsm2d(vt, Zr, src, s, 1, 500, 10.0, 10.0)
+        a = port.rt_fsm2d(vt, Z, src, s, 2, maxswp, 10.0, 10.0)
+        b = ref.rt_fsm2d(vt, Z, src, s, 2, maxswp, 10.0, 10.0)
         assert a[3] == 0
         for x, y in zip(a[:3], b):
             assert bits_equal(x, y)
         rng = np.random.default_rng(s)
         tt = a[0][rec[:, 0], rec[:, 1]] + rng.normal(0, 1e-3, len(rec))
-        tr = np.stack([a[2][0][rec[:, 0], rec[:, 1]] + rng.normal(0, 1e-3, len(rec))], 1)
-        tr[::7] = 0.0    # unpicked reflections
-        L, E, _ = port.tadjoint2d(a[0], tt, rec, nxy, src, srnum, s, 500, 10.0, 10.0)
-        Lr, Er = ref.tadjoint2d(a[0], tt, rec, nxy, src, srnum, s, 500, 10.0, 10.0)
+        tr = np.stack([a[2][k][rec[:, 0], rec[:, 1]] + rng.normal(0, 1e-3, len(rec)) for k in range(2)], 1)
+        tr[::7, 0] = 0.0    # unpicked reflections
+        L, E, _ = port.tadjoint2d(a[0], tt, rec, nxy, src, srnum, s, maxswp, 10.0, 10.0)
+        Lr, Er = ref.tadjoint2d(a[0], tt, rec, nxy, src, srnum, s, maxswp, 10.0, 10.0)
         assert bits_equal(L, Lr) and E == Er
-        R, E2, _ = port.radjoint2d(a[2], tr, rec, nxy, src, srnum, s, 1, 500, 10.0, 10.0)
-        Rr, E2r = ref.radjoint2d(a[1], a[2], tr, rec, nxy, src, srnum, s, 1, 500, 10.0, 10.0)
+        R, E2, _ = port.radjoint2d(a[2], tr, rec, nxy, src, srnum, s, 2, maxswp, 10.0, 10.0)
+        Rr, E2r = ref.radjoint2d(a[1], a[2], tr, rec, nxy, src, srnum, s, 2, maxswp, 10.0, 10.0)
         assert bits_equal(R, Rr) and E2 == E2r
 
 
