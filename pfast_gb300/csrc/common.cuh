@@ -29,7 +29,7 @@ static_assert(PS >= HI * HJ && (PS - 1) % 32 == 8 && (HJ - 1) % 32 == 1, "bank-c
 constexpr int SJ = TJ + 2, SPS = 297;
 static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
 // Warps (tiles) per CTA.
-constexpr int kWarps3 = 4;
+constexpr int kWarps3 = 1;   // one-warp CTAs: the finest shared-memory granularity, hence the most warps per SM
 
 // ---------------------------------------------------------------- 2D tiles
 // One warp sweeps one T2I x T2J tile; lane = row, pencil along j.
@@ -47,7 +47,21 @@ struct Spacing3 {
     double d[3];
     double d2[3];    // d*d
     double inv2[3];  // (1.0/d)/d
+    // FP32 constants of the fast kernels, computed on the host so that no FP64
+    // instruction runs in an FP32 kernel: w = 1/d^2, rp[a] = 1/(W - w[a]), rW = 1/W.
+    float df[3], wf[3], rpf[3], rWf;
+    int iso;         // dx == dy == dz
 };
+
+// Bit-pattern helpers.  For doubles >= +0 (including +inf) the IEEE bit patterns
+// order like the values, so comparisons and minima of traveltimes can run on the
+// integer pipe (FP64 issue slots are scarce on this part).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+// (x < y) ? x : y for x, y >= +0: the reference's MIN macro
+__device__ __forceinline__ double min_nonneg(double x, double y) { return dbits(x) < dbits(y) ? x : y; }
+// max(e, 0) and min(e, 0) by the sign bit
+__device__ __forceinline__ double pos_sign(double e) { return __double2hiint(e) < 0 ? 0.0 : e; }
+__device__ __forceinline__ double neg_sign(double e) { return __double2hiint(e) < 0 ? e : 0.0; }
 
 // Which kernel flavour a sweep runs.
 enum SweepKind : int {

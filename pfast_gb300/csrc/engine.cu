@@ -119,12 +119,21 @@ constexpr double kTol32AbsAdj = 1e-6;
 
 Spacing3 make_spacing(double dx, double dy, double dz) {
     Spacing3 s;
+    std::memset(&s, 0, sizeof(s));
     const double d[3] = {dx, dy, dz};
     for (int a = 0; a < 3; ++a) {
         s.d[a] = d[a];
         s.d2[a] = d[a] * d[a];
         s.inv2[a] = 1.0 / d[a] / d[a];
     }
+    const double W = s.inv2[0] + s.inv2[1] + s.inv2[2];
+    for (int a = 0; a < 3; ++a) {
+        s.df[a] = (float)d[a];
+        s.wf[a] = (float)s.inv2[a];
+        s.rpf[a] = (float)(1.0 / (W - s.inv2[a]));
+    }
+    s.rWf = (float)(1.0 / W);
+    s.iso = (dx == dy && dy == dz) ? 1 : 0;
     return s;
 }
 
@@ -195,6 +204,26 @@ Sweep3Args base_args(const pfast_survey3d* sv) {
 
 }  // namespace
 
+pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed) {
+    PFAST_TRY(ctx->s64.ensure(sizeof(double) * N));
+    if (mixed) {
+        PFAST_TRY(ctx->s32.ensure(sizeof(float) * N));
+        PFAST_TRY(ctx->sq64.ensure(sizeof(double) * N));
+    }
+    PFAST_TRY(ctx->need.ensure(sizeof(int) * 4));
+    PFAST_CUDA_TRY(cudaMemsetAsync(ctx->need.p, 0, sizeof(int), ctx->stream));
+    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), mixed ? ctx->s32.as<float>() : nullptr,
+                                      mixed ? ctx->sq64.as<double>() : nullptr, ctx->need.as<int>(), N, ctx->stream));
+    int bad = 0;
+    PFAST_CUDA_TRY(cudaMemcpyAsync(&bad, ctx->need.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PFAST_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (bad) {
+        set_last_error("the velocity model holds a value that is not a positive finite number");
+        return PFAST_ERR_INVALID;
+    }
+    return PFAST_OK;
+}
+
 pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, int nb, int precision, int maxswp,
                              pfast_stats* st) {
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
@@ -234,8 +263,8 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.field = T32;
         a.snap = snap32;
         a.aux = ctx->s32.p;
-        a.tol_abs = 0.0;
-        a.tol_rel = kTol32Rel;
+        a.tol_abs_f = 0.0f;
+        a.tol_rel_f = (float)kTol32Rel;
         PFAST_TRY(run_sweeps3(ctx, a, kFwdFast32, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
                               st ? &st->ms_fwd32 : nullptr));
         if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
@@ -245,7 +274,8 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = ctx->T64.p;
         a.snap = ctx->scratch.p;
-        a.aux = ctx->s64.p;
+        a.aux = ctx->sq64.p;
+        a.slow64 = ctx->s64.as<double>();
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
@@ -335,11 +365,14 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         std::vector<int> active64 = active;
         float* L32 = ctx->scratch.as<float>();
         float* snap32 = L32 + N * nb;
+        PFAST_TRY(ctx->T32.ensure(sizeof(float) * N * nb));
         PFAST_LAUNCH(ctx, launch_narrow(ctx->L64.as<double>(), L32, N, N, N, nb, s));
+        PFAST_LAUNCH(ctx, launch_narrow(ctx->T64.as<double>(), ctx->T32.as<float>(), N, N, N, nb, s));
         a.field = L32;
         a.snap = snap32;
-        a.tol_abs = kTol32AbsAdj;
-        a.tol_rel = kTol32Rel;
+        a.aux = ctx->T32.p;
+        a.tol_abs_f = (float)kTol32AbsAdj;
+        a.tol_rel_f = (float)kTol32Rel;
         PFAST_TRY(run_sweeps3(ctx, a, kAdjFast32, *dt, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
                               st ? &st->ms_adj32 : nullptr));
         if (st) for (int v : iters) st->adj32_iters_max = std::max(st->adj32_iters_max, v);
@@ -348,6 +381,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         std::fill(iters.begin(), iters.end(), 0);
         a.field = ctx->L64.p;
         a.snap = ctx->scratch.p;
+        a.aux = ctx->T64.p;
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
@@ -462,7 +496,7 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
     if (!ctx) return PFAST_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
+    for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->sq64, &ctx->T32, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
                       &ctx->ee, &ctx->need, &ctx->misc, &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a,
                       &ctx->f2b, &ctx->f2c})
         b->release();
@@ -593,9 +627,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     cudaEvent_t t0 = ctx->ev[6], t1 = ctx->ev[7];
     PFAST_CUDA_TRY(cudaEventRecord(t0, s));
     const long long launches0 = ctx->launches;
-    PFAST_TRY(ctx->s64.ensure(sizeof(double) * N));
-    PFAST_TRY(ctx->s32.ensure(sizeof(float) * N));
-    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), o.precision == PFAST_MIXED ? ctx->s32.as<float>() : nullptr, N, s));
+    PFAST_TRY(prepare_slowness(ctx, vp, N, o.precision == PFAST_MIXED));
     if (want_grad) PFAST_CUDA_TRY(cudaMemsetAsync(grad, 0, sizeof(double) * N, s));
     const size_t per_src = (size_t)N * (want_grad ? 24 : 16) + (size_t)sv->nz * sv->nr * ((sv->nc + 31) / 32) * 4;
     const int B = pick_batch(std::max(sv->nsrc, 1), o.max_batch, per_src);
@@ -721,8 +753,7 @@ pfast_status pfast_fsm3d(double* vp, double* U, int* src, int srcid, int MAXSwp,
         cudaError_t e = cudaMemcpyAsync(ctx->vp_tmp.p, vp, sizeof(double) * N, cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) r = cuda_fail(e, "copy vp", __FILE__, __LINE__);
     }
-    if (!r) r = ctx->s64.ensure(sizeof(double) * N);
-    if (!r) r = launch_slowness(ctx->vp_tmp.as<double>(), ctx->s64.as<double>(), nullptr, N, s);
+    if (!r) r = prepare_slowness(ctx, ctx->vp_tmp.as<double>(), N, false);
     if (!r) r = forward3d_batch(ctx, sv, 0, 1, PFAST_PLAIN_FP64, MAXSwp, nullptr);
     if (!r) {
         cudaError_t e = cudaMemcpyAsync(U, ctx->T64.p, sizeof(double) * N, cudaMemcpyDeviceToHost, s);

@@ -41,7 +41,7 @@ struct pfast_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     // device work buffers (reused across calls)
-    pfast::DevBuf s64, s32, T64, L64, scratch, mask, act, changed, ee, need, misc, grad_tmp, vp_tmp, picks_tmp;
+    pfast::DevBuf s64, s32, sq64, T32, T64, L64, scratch, mask, act, changed, ee, need, misc, grad_tmp, vp_tmp, picks_tmp;
     pfast::DevBuf f2a, f2b, f2c;       // 2D field buffers
     pfast::HostBuf h_act, h_changed, h_ee, h_need;
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
@@ -105,6 +105,10 @@ pfast_status ctx_diag2(pfast_ctx* ctx, int nr, int nc, DiagTable2** out);
 
 // The process-wide context of the calling thread's current device (reference shims).
 pfast_status default_context(pfast_ctx** out);
+
+// Slowness arrays of a model (s64 always; s32 and s^2 for the mixed mode); rejects a
+// model with a non-positive or non-finite velocity.
+pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed);
 
 // Time between two recorded events, added to *acc (ms).
 void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc);

@@ -508,9 +508,7 @@ pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp
     cudaStream_t s = ctx->stream;
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[6], s));
     const long long l0 = ctx->launches;
-    PFAST_TRY2(ctx->s64.ensure(sizeof(double) * N));
-    PFAST_TRY2(ctx->s32.ensure(sizeof(float) * N));
-    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), ctx->s32.as<float>(), N, s));
+    PFAST_TRY2(prepare_slowness(ctx, vp, N, true));
     const size_t per_src = (size_t)N * 8 * (1 + 2 * R) + (size_t)N * 16 * (1 + R);
     const int B = pick_batch2(std::max(sv->nsrc, 1), (TTd_host || TT_host) ? 1 : o.max_batch, per_src);
     for (int b0 = 0; b0 < sv->nsrc; b0 += B) {
@@ -562,9 +560,7 @@ pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, c
     cudaStream_t s = ctx->stream;
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[6], s));
     const long long l0 = ctx->launches;
-    PFAST_TRY2(ctx->s64.ensure(sizeof(double) * N));
-    PFAST_TRY2(ctx->s32.ensure(sizeof(float) * N));
-    PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), ctx->s32.as<float>(), N, s));
+    PFAST_TRY2(prepare_slowness(ctx, vp, N, true));
     PFAST_CUDA_TRY(cudaMemsetAsync(gT, 0, sizeof(double) * N, s));
     PFAST_CUDA_TRY(cudaMemsetAsync(gR, 0, sizeof(double) * N, s));
     const size_t per_src = (size_t)N * 8 * (1 + 2 * R + 3) + (size_t)N * 16 * (1 + R);

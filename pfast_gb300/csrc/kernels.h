@@ -12,7 +12,10 @@ namespace pfast {
 struct Sweep3Args {
     void* field;              // Real fields, per instance
     long long fstride;        // elements between instances (same for snap / aux / T)
-    const void* aux;          // forward: slowness (shared, Real); adjoint: T (double, per instance)
+    const void* aux;          // plain forward: slowness 1/vp (double); FP32 forward: slowness (float);
+                              // polish forward: slowness squared (double); adjoint: T per instance
+                              // (double, or float for the FP32 adjoint)
+    const double* slow64;     // polish forward: slowness (double), for the restart branch
     const unsigned* mask;     // adjoint: fixed-node bits, per instance, mask_stride words apart
     long long mask_stride;
     int wpr;                  // mask words per grid row
@@ -27,7 +30,8 @@ struct Sweep3Args {
     Spacing3 sp;
     int dir;                  // sweep order 0..7: bit2 = s3>0 (z), bit1 = s1>0 (rows), bit0 = s2>0 (cols)
     int first, last;          // first / last sweep of an outer iteration
-    double tol_abs, tol_rel;  // change test: |new-old| > tol_abs + tol_rel*|new|
+    double tol_abs, tol_rel;  // change test: |new-old| > tol_abs + tol_rel*|new| (FP64 sweeps)
+    float tol_abs_f, tol_rel_f;  // the same test for the FP32 sweeps, evaluated in FP32
 };
 
 // Tile-diagonal table for a grid: tiles (bk, bi, bj) in flipped coordinates with
@@ -46,7 +50,10 @@ size_t sweep3_smem_bytes(int kind);
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
 
 // Small 3D kernels.
-pfast_status launch_slowness(const double* vp, double* s64, float* s32, long long n, cudaStream_t st);
+// s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64 (if non-null); *bad is set
+// when some vp is not a positive finite number.
+pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, int* bad, long long n,
+                             cudaStream_t st);
 pfast_status launch_init_fwd3(void* field, int is_fp32, long long fstride, long long n, const long long* src_lin,
                               int nbatch, cudaStream_t st);
 pfast_status launch_widen(const float* src, double* dst, long long fstride32, long long fstride64, long long n,

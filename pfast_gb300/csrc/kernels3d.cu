@@ -11,9 +11,11 @@
 //
 // Flavours: kFwdPlain64 / kAdjPlain64 evaluate the reference's expressions in the
 // reference's order (the library is built with -fmad=false, so no FMA contraction):
-// bit-identical results.  kFwdFast32 / kAdjFast32 (bulk) and kFwdPolish64 /
-// kAdjPolish64 (polish) use the same Godunov / upwind-adjoint updates written with
-// precomputed reciprocals and a cancellation-free quadratic.
+// bit-identical results.  kFwdFast32 / kAdjFast32 are the FP32 bulk sweeps and run
+// no FP64 instruction.  kFwdPolish64 / kAdjPolish64 are the FP64 polish sweeps in
+// residual-correction form: the local residual is formed in FP64 and the correction
+// step in FP32, so the fixed point is the FP64 one while FP64 issue slots (about 2
+// lanes per clock per SM on this part) go only where the precision is needed.
 
 #include <vector>
 #include <algorithm>
@@ -40,29 +42,28 @@ __host__ __device__ constexpr int warp_smem_bytes() {
                (T::adj ? HK * PS * sizeof(typename T::Aux) : TK * SPS * sizeof(typename T::Aux)));
 }
 
-__device__ __forceinline__ double ref_min(double x, double y) { return (x < y) ? x : y; }  // MIN macro
 __device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
 
 // ----------------------------------------------------------- node updates
 // Reference Godunov update (src/T_pfsm3d.h:99-119).  a/b/c: neighbour minima along
 // x/y/z; s: slowness 1.0/vp (precomputed, bit-identical to the reference's per-node
-// division).  Expressions keep the reference's operand order.
+// division).  Expressions keep the reference's operand order; the ordering tests
+// run on the bit patterns (same outcome for non-negative values).
 __device__ __forceinline__ double eik3_plain(double a, double b, double c, double s, const Spacing3& sp) {
     double da = sp.d[0], db = sp.d[1], dc = sp.d[2];
     double ia = sp.inv2[0], ib = sp.inv2[1], ic = sp.inv2[2];
     double t;
-    if (b > a) { t = a; a = b; b = t; t = da; da = db; db = t; t = ia; ia = ib; ib = t; }
-    if (c > a) { t = a; a = c; c = t; t = da; da = dc; dc = t; t = ia; ia = ic; ic = t; }
-    if (c > b) { t = b; b = c; c = t; t = db; db = dc; dc = t; t = ib; ib = ic; ic = t; }
-    if (!(c <= b && b <= a)) return 0.0;
+    if (dbits(b) > dbits(a)) { t = a; a = b; b = t; t = da; da = db; db = t; t = ia; ia = ib; ib = t; }
+    if (dbits(c) > dbits(a)) { t = a; a = c; c = t; t = da; da = dc; dc = t; t = ia; ia = ic; ic = t; }
+    if (dbits(c) > dbits(b)) { t = b; b = c; c = t; t = db; db = dc; dc = t; t = ib; ib = ic; ic = t; }
     double q = dc * s + c;
-    if (q <= b) return q;
+    if (dbits(q) <= dbits(b)) return q;
     double A = dc * dc + db * db;
     double B = -2. * (b * dc * dc + c * db * db);
     double C = dc * dc * b * b + db * db * c * c - db * db * dc * dc * s * s;
     double D = B * B - 4. * A * C;
     q = (D >= 0) ? (-B + sqrt(D)) / 2. / A : kInf;
-    if (q <= a) return q;
+    if (dbits(q) <= dbits(a)) return q;
     A = ia + ib + ic;   // 1.0/da/da + 1.0/db/db + 1.0/dc/dc, each term precomputed as (1.0/d)/d
     B = -2.0 * (a / da / da + b / db / db + c / dc / dc);
     C = a * a / da / da + b * b / db / db + c * c / dc / dc - s * s;
@@ -71,64 +72,80 @@ __device__ __forceinline__ double eik3_plain(double a, double b, double c, doubl
     return q;
 }
 
-// Constants of the fast Godunov form: w = 1/d^2 per axis, rp[ax] = 1/(W - w[ax]) (the
-// pair of the two other axes), rW = 1/W with W = sum w.
-template <typename R> struct FastConst {
-    R d[3], w[3], rp[3], rW;
-};
-
-template <typename R>
-__device__ __forceinline__ FastConst<R> fast_const(const Spacing3& sp) {
-    FastConst<R> k;
-    double W = sp.inv2[0] + sp.inv2[1] + sp.inv2[2];
-    for (int a = 0; a < 3; ++a) {
-        k.d[a] = (R)sp.d[a];
-        k.w[a] = (R)sp.inv2[a];
-        k.rp[a] = (R)(1.0 / (W - sp.inv2[a]));
-    }
-    k.rW = (R)(1.0 / W);
-    return k;
-}
-
-// Same Godunov solution as eik3_plain, in difference form relative to the smallest
-// neighbour c (x = q - c), with FMA and reciprocal multiplies:
+// FP32 Godunov solution in difference form relative to the smallest neighbour c
+// (x = q - c), with FMA and host-precomputed reciprocals:
 //   1 term:  x = dc*s
 //   2 terms: x = (wb*B + sqrt((wb+wc) s^2 - wb wc B^2)) / (wb+wc),         B = b-c
 //   3 terms: x = (wa*A + wb*B + sqrt(W s^2 - wa wb (A-B)^2 - wa wc A^2 - wb wc B^2)) / W,  A = a-c
-template <typename R>
-__device__ __forceinline__ R eik3_fast(R a, R b, R c, R s, const FastConst<R>& K) {
-    R da = K.d[0], db = K.d[1], dc = K.d[2];
-    R wa = K.w[0], wb = K.w[1], wc = K.w[2];
-    R ra = K.rp[0], rb = K.rp[1], rc = K.rp[2];
-    R t;
+__device__ __forceinline__ float eik3_fast(float a, float b, float c, float s, const Spacing3& K) {
+    float da = K.df[0], db = K.df[1], dc = K.df[2];
+    float wa = K.wf[0], wb = K.wf[1], wc = K.wf[2];
+    float ra = K.rpf[0], rb = K.rpf[1], rc = K.rpf[2];
+    float t;
     if (b > a) { t = a; a = b; b = t; t = da; da = db; db = t; t = wa; wa = wb; wb = t; t = ra; ra = rb; rb = t; }
     if (c > a) { t = a; a = c; c = t; t = da; da = dc; dc = t; t = wa; wa = wc; wc = t; t = ra; ra = rc; rc = t; }
     if (c > b) { t = b; b = c; c = t; t = db; db = dc; dc = t; t = wb; wb = wc; wc = t; t = rb; rb = rc; rc = t; }
-    R q = fma(dc, s, c);
+    float q = fmaf(dc, s, c);
     if (q <= b) return q;
-    const R s2 = s * s;
-    const R B = b - c;
-    const R wbB = wb * B;
-    R D = fma(wb + wc, s2, -wbB * wc * B);
-    q = (D >= R(0)) ? c + (wbB + sqrt(D)) * ra : R(kInf);
+    const float s2 = s * s;
+    const float B = b - c;
+    const float wbB = wb * B;
+    const float D = fmaf(wb + wc, s2, -wbB * wc * B);
+    q = (D >= 0.f) ? c + (wbB + sqrtf(D)) * ra : (float)kInf;
     if (q <= a) return q;
-    const R A = a - c;
-    const R AB = A - B;
-    const R W = wa + wb + wc;
-    R D3 = W * s2 - (wa * wb * AB * AB + wa * wc * A * A + wb * wc * B * B);
-    q = (D3 >= R(0)) ? c + (fma(wa, A, wbB) + sqrt(D3)) * K.rW : R(kInf);
-    return q;
+    const float A = a - c;
+    const float AB = A - B;
+    const float W = wa + wb + wc;
+    const float D3 = W * s2 - (wa * wb * AB * AB + wa * wc * A * A + wb * wc * B * B);
+    return (D3 >= 0.f) ? c + (fmaf(wa, A, wbB) + sqrtf(D3)) * K.rWf : (float)kInf;
 }
 
-__device__ __forceinline__ double pos_ref(double x) { return (x + fabs(x)) / 2.0; }   // POS macro
-__device__ __forceinline__ double neg_ref(double x) { return (x - fabs(x)) / 2.0; }   // NEG macro
+// FP64 polish Godunov update: one Newton step from the current value U0 on
+//   f(q) = sum_m w_m max(q - a_m, 0)^2 - s^2,
+// whose root is the Godunov value (the 1-, 2- and 3-term cases of
+// src/T_pfsm3d.h:106-118 are the pieces of f).  f in FP64, the step f/f' in FP32.
+// s2 = s^2 (precomputed); the rare restart branch (U0 at or below every
+// neighbour) takes the 1-term value with the slowness itself.
+__device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s2, const double* slow,
+                                              long long node, const Spacing3& sp) {
+    const double px = pos_sign(U0 - a), py = pos_sign(U0 - b), pz = pos_sign(U0 - c);
+    double f, g;
+    if (sp.iso) {
+        f = fma(sp.inv2[0], fma(px, px, fma(py, py, pz * pz)), -s2);
+        g = (px + py) + pz;
+    } else {
+        f = fma(sp.inv2[0] * px, px, fma(sp.inv2[1] * py, py, fma(sp.inv2[2] * pz, pz, -s2)));
+        g = 0.0;
+    }
+    float fp;
+    if (sp.iso) fp = 2.0f * sp.wf[0] * (float)g;
+    else fp = 2.0f * (sp.wf[0] * (float)px + sp.wf[1] * (float)py + sp.wf[2] * (float)pz);
+    if (!(fp > 0.0f)) {
+        const double s = __ldg(slow + node);
+        return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
+    }
+    return U0 - (double)__fdividef((float)f, fp);
+}
+
+// Adjoint updates.  The reference's upwind formula (src/T_padjoint3d.h:51-66)
+// collapses, with w = 1/d^2 of each neighbour's axis and e_m = T_m - T0, to
+//   den = sum_m w_m max(-e_m, 0),   num = sum_m w_m max(e_m, 0) lambda_m,   lambda = num / den
+// (POS(-(T_p-T0)/d)/d = w max(-e_p,0), -NEG(-(T0-T_m)/d)/d = w max(-e_m,0),
+//  POS(-(T0-T_m)/d)/d = w max(e_m,0), -NEG(-(T_p-T0)/d)/d = w max(e_p,0)).
 
 // Reference adjoint update (src/T_padjoint3d.h:42-71); operand order kept.
+__device__ __forceinline__ double pos_ref(double x) { return (x + fabs(x)) / 2.0; }   // POS macro
+__device__ __forceinline__ double neg_ref(double x) { return (x - fabs(x)) / 2.0; }   // NEG macro
+__device__ __forceinline__ bool unreached64(double T0, double a, double b, double c, double d, double e, double f) {
+    const long long inf = dbits(kInf);   // T >= INF, on the bit patterns (T >= 0)
+    return dbits(T0) >= inf || dbits(a) >= inf || dbits(b) >= inf || dbits(c) >= inf || dbits(d) >= inf ||
+           dbits(e) >= inf || dbits(f) >= inf;
+}
+
 __device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, double Typ, double Tym,
                                              double Tzp, double Tzm, double Lxp, double Lxm, double Lyp,
                                              double Lym, double Lzp, double Lzm, const Spacing3& sp) {
-    if (T0 >= kInf || Txp >= kInf || Txm >= kInf || Typ >= kInf || Tym >= kInf || Tzp >= kInf || Tzm >= kInf)
-        return 0.0;
+    if (unreached64(T0, Txp, Txm, Typ, Tym, Tzp, Tzm)) return 0.0;
     const double dx = sp.d[0], dy = sp.d[1], dz = sp.d[2];
     const double gxp = -(Txp - T0) / dx, gxm = -(T0 - Txm) / dx;
     const double gyp = -(Typ - T0) / dy, gym = -(T0 - Tym) / dy;
@@ -144,80 +161,62 @@ __device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, 
     return 0.0;
 }
 
-// Fast adjoint update.  The reference's upwind formula (src/T_padjoint3d.h:51-66)
-// collapses, with w = 1/d^2 of each neighbour's axis and e_m = T_m - T0, to
-//   den = sum_m w_m max(-e_m, 0),   num = sum_m w_m max(e_m, 0) lambda_m,   lambda = num / den
-// (POS(-(T_p-T0)/d) = max(-e_p,0)/d, -NEG(-(T0-T_m)/d) = max(-e_m,0)/d, and so on).
-// T values may be offsets from a common reference; an unreached node has T >= tinf.
-template <typename R>
-__device__ __forceinline__ void adj3_terms(R T0, R Txp, R Txm, R Typ, R Tym, R Tzp, R Tzm, R Lxp, R Lxm, R Lyp,
-                                           R Lym, R Lzp, R Lzm, R wx, R wy, R wz, R& num, R& den) {
-    const R z = R(0);
-    R e;
-    e = Txp - T0; den = wx * fmax(-e, z); num = wx * fmax(e, z) * Lxp;
-    e = Txm - T0; den = fma(wx, fmax(-e, z), den); num = fma(wx * fmax(e, z), Lxm, num);
-    e = Typ - T0; den = fma(wy, fmax(-e, z), den); num = fma(wy * fmax(e, z), Lyp, num);
-    e = Tym - T0; den = fma(wy, fmax(-e, z), den); num = fma(wy * fmax(e, z), Lym, num);
-    e = Tzp - T0; den = fma(wz, fmax(-e, z), den); num = fma(wz * fmax(e, z), Lzp, num);
-    e = Tzm - T0; den = fma(wz, fmax(-e, z), den); num = fma(wz * fmax(e, z), Lzm, num);
-}
-
-template <typename R>
-__device__ __forceinline__ bool any_unreached(R T0, R a, R b, R c, R d, R e, R f, R tinf) {
-    return T0 >= tinf || a >= tinf || b >= tinf || c >= tinf || d >= tinf || e >= tinf || f >= tinf;
-}
-
-// FP32 bulk adjoint update.
+// FP32 bulk adjoint update (T as FP32 values; unreached nodes hold INF).
 __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float Typ, float Tym, float Tzp, float Tzm,
-                                           float Lxp, float Lxm, float Lyp, float Lym, float Lzp, float Lzm, float wx,
-                                           float wy, float wz) {
-    if (any_unreached(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, INFINITY)) return 0.f;
-    float num, den;
-    adj3_terms<float>(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, wx, wy, wz, num, den);
+                                           float Lxp, float Lxm, float Lyp, float Lym, float Lzp, float Lzm,
+                                           const Spacing3& sp) {
+    const float ti = (float)kInf;
+    if (T0 >= ti || Txp >= ti || Txm >= ti || Typ >= ti || Tym >= ti || Tzp >= ti || Tzm >= ti) return 0.f;
+    const float wx = sp.wf[0], wy = sp.wf[1], wz = sp.wf[2];
+    float e, den, num;
+    e = Txp - T0; den = wx * fmaxf(-e, 0.f); num = wx * fmaxf(e, 0.f) * Lxp;
+    e = Txm - T0; den = fmaf(wx, fmaxf(-e, 0.f), den); num = fmaf(wx * fmaxf(e, 0.f), Lxm, num);
+    e = Typ - T0; den = fmaf(wy, fmaxf(-e, 0.f), den); num = fmaf(wy * fmaxf(e, 0.f), Lyp, num);
+    e = Tym - T0; den = fmaf(wy, fmaxf(-e, 0.f), den); num = fmaf(wy * fmaxf(e, 0.f), Lym, num);
+    e = Tzp - T0; den = fmaf(wz, fmaxf(-e, 0.f), den); num = fmaf(wz * fmaxf(e, 0.f), Lzp, num);
+    e = Tzm - T0; den = fmaf(wz, fmaxf(-e, 0.f), den); num = fmaf(wz * fmaxf(e, 0.f), Lzm, num);
     return (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
 }
 
-// FP64 polish adjoint update in residual-correction form: the residual
-// r = num - den*lambda0 is formed in FP64, the correction r/den in FP32.
+// FP64 polish adjoint update in residual-correction form: num, den and the residual
+// r = num - den*lambda0 in FP64 (max(+-e, 0) by the sign bit), the step r/den in FP32.
 __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm, double Typ, double Tym, double Tzp,
                                               double Tzm, double Lxp, double Lxm, double Lyp, double Lym, double Lzp,
-                                              double Lzm, double L0, double wx, double wy, double wz) {
-    if (any_unreached(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, kInf)) return 0.0;
-    double num, den;
-    adj3_terms<double>(T0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, wx, wy, wz, num, den);
-    if (!(fabs(den) > 1e-9)) return 0.0;
+                                              double Lzm, double L0, const Spacing3& sp) {
+    if (unreached64(T0, Txp, Txm, Typ, Tym, Tzp, Tzm)) return 0.0;
+    const double exp_ = Txp - T0, exm = Txm - T0, eyp = Typ - T0, eym = Tym - T0, ezp = Tzp - T0, ezm = Tzm - T0;
+    double num, den;   // den is accumulated with the sign flipped: -sum w min(e, 0)
+    if (sp.iso) {
+        den = ((neg_sign(exp_) + neg_sign(exm)) + (neg_sign(eyp) + neg_sign(eym))) + (neg_sign(ezp) + neg_sign(ezm));
+        num = fma(pos_sign(exp_), Lxp, fma(pos_sign(exm), Lxm, fma(pos_sign(eyp), Lyp,
+              fma(pos_sign(eym), Lym, fma(pos_sign(ezp), Lzp, pos_sign(ezm) * Lzm)))));
+        den = -sp.inv2[0] * den;
+        num = sp.inv2[0] * num;
+    } else {
+        const double wx = sp.inv2[0], wy = sp.inv2[1], wz = sp.inv2[2];
+        den = -(wx * (neg_sign(exp_) + neg_sign(exm)) + wy * (neg_sign(eyp) + neg_sign(eym)) +
+                wz * (neg_sign(ezp) + neg_sign(ezm)));
+        num = wx * fma(pos_sign(exp_), Lxp, pos_sign(exm) * Lxm) + wy * fma(pos_sign(eyp), Lyp, pos_sign(eym) * Lym) +
+              wz * fma(pos_sign(ezp), Lzp, pos_sign(ezm) * Lzm);
+    }
+    if (!(dbits(den) > dbits(1e-9))) return 0.0;   // den >= 0 by construction
     const double r = fma(-den, L0, num);
     return L0 + (double)__fdividef((float)r, (float)den);
-}
-
-// FP64 polish Godunov update in residual-correction form: one Newton step from the
-// current value U0 on f(q) = sum_m w_m max(q - a_m, 0)^2 - s^2, whose root is the
-// Godunov value (the 1-, 2- and 3-term cases of src/T_pfsm3d.h:106-118 are the
-// pieces of this function).  f is evaluated in FP64, the step f / f' in FP32.
-__device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s, const Spacing3& sp) {
-    const double px = fmax(U0 - a, 0.0), py = fmax(U0 - b, 0.0), pz = fmax(U0 - c, 0.0);
-    const double wx = sp.inv2[0], wy = sp.inv2[1], wz = sp.inv2[2];
-    const double f = fma(wx * px, px, fma(wy * py, py, fma(wz * pz, pz, -s * s)));
-    const float fp = 2.0f * ((float)wx * (float)px + (float)wy * (float)py + (float)wz * (float)pz);
-    if (!(fp > 0.0f)) {   // U0 at or below every neighbour: restart from the 1-term value
-        return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
-    }
-    return U0 - (double)__fdividef((float)f, fp);
 }
 
 // ----------------------------------------------------------- tile I/O
 // Load the (TK+2)x(TI+2)x(TJ+2) halo box at origin (k0-1, i0-1, j0-1) into `box`
 // (plane stride PS, row stride HJ).  Out-of-grid entries get `fill`.  Loads are
 // issued 16 per lane before their shared-memory stores, to keep many in flight.
-template <typename Dst, typename Src, typename Conv>
-__device__ __forceinline__ void load_box(Dst* box, const Src* __restrict__ g, int k0, int i0, int j0, int nz, int nr,
-                                         int nc, Dst fill, int lane, Conv conv) {
+template <typename T>
+__device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0, int i0, int j0, int nz, int nr,
+                                         int nc, T fill, int lane) {
     constexpr int NE = HK * HI * HJ;
     constexpr int BATCH = 16;
     const long long plane = (long long)nr * nc;
 #pragma unroll 1
     for (int base = 0; base < NE; base += 32 * BATCH) {
-        Dst v[BATCH];
+        T v[BATCH];
 #pragma unroll
         for (int u = 0; u < BATCH; ++u) {
             const int e = base + u * 32 + lane;
@@ -227,7 +226,7 @@ __device__ __forceinline__ void load_box(Dst* box, const Src* __restrict__ g, in
                 const int z = r / HI, y = r - z * HI;
                 const int gk = k0 - 1 + z, gi = i0 - 1 + y, gj = j0 - 1 + x;
                 if ((unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr && (unsigned)gj < (unsigned)nc)
-                    v[u] = conv(g[gk * plane + (long long)gi * nc + gj]);
+                    v[u] = __ldg(g + gk * plane + (long long)gi * nc + gj);
             }
         }
 #pragma unroll
@@ -241,10 +240,6 @@ __device__ __forceinline__ void load_box(Dst* box, const Src* __restrict__ g, in
         }
     }
 }
-
-struct Ident {
-    template <typename T> __device__ __forceinline__ T operator()(T v) const { return v; }
-};
 
 // ----------------------------------------------------------- the sweep kernel
 template <int KIND>
@@ -280,37 +275,26 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     // ---- stage the field halo box (out-of-grid: +inf for the forward so that the
     // neighbour minimum reduces to the one-sided rule at faces; never read by the adjoint)
     const Real fill = ADJ ? Real(0) : Real(INFINITY);
-    load_box(box, fld, k0, i0, j0, nz, nr, nc, fill, lane, Ident());
+    load_box<Real>(box, fld, k0, i0, j0, nz, nr, nc, fill, lane);
 
     // ---- auxiliary data
-    double tref = 0.0;
     unsigned fixed_bits = 0;
     const int lkf = lane / TI, lif = lane % TI;
     const bool lane_ok = lkf < ek && lif < ei;
     const int lk = pz ? lkf : ek - 1 - lkf;
     const int li = py ? lif : ei - 1 - lif;
     if constexpr (!ADJ) {
-        // slowness tile [lk][li][lj], rows loaded coalesced
+        // slowness (or its square) tile [lk][li][lj], rows loaded coalesced, 8 rows in flight
         const Aux* s = reinterpret_cast<const Aux*>(A.aux);
 #pragma unroll 8
         for (int m = 0; m < 32; ++m) {
             const int rk = m / TI, ri = m % TI;
             if (rk < ek && ri < ei && lane < ej)
-                aux[rk * SPS + ri * SJ + lane] = s[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane];
+                aux[rk * SPS + ri * SJ + lane] = __ldg(s + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane);
         }
     } else {
-        const double* T = reinterpret_cast<const double*>(A.aux) + inst * A.fstride;
-        if constexpr (sizeof(Aux) == 8) {
-            load_box(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane, Ident());
-        } else {
-            // FP32 bulk: offsets from one reference time of the tile keep the
-            // differences accurate; unreached nodes become +inf
-            tref = T[(long long)k0 * plane + (long long)i0 * nc + j0];
-            if (tref >= kInf) tref = 0.0;
-            const double tr = tref;
-            load_box(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane,
-                     [tr](double v) { return v >= kInf ? (Aux)INFINITY : (Aux)(v - tr); });
-        }
+        const Aux* T = reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride;
+        load_box<Aux>(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane);
         if (lane_ok)
             fixed_bits = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
     }
@@ -334,10 +318,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     int sk = -1, si = -1, sj = -1;
     if constexpr (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
     const bool row_interior = ADJ ? (gk >= 1 && gk <= nz - 2 && gi >= 1 && gi <= nr - 2) : true;
-
-    FastConst<float> K;
-    if constexpr (KIND == kFwdFast32) K = fast_const<float>(A.sp);
-    const float wx32 = (float)A.sp.inv2[0], wy32 = (float)A.sp.inv2[1], wz32 = (float)A.sp.inv2[2];
+    const long long rowbase = gk * plane + (long long)gi * nc;
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
@@ -348,18 +329,23 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
             const int gj = j0 + lj;
             if constexpr (!ADJ) {
                 if (!(gk == sk && gi == si && gj == sj)) {
-                    const Real xa = ref_min(box[c + 1], box[c - 1]);
-                    const Real yb = ref_min(box[c - HJ], box[c + HJ]);
-                    const Real zc = ref_min(box[c - PS], box[c + PS]);
-                    const Real s = aux[lk * SPS + li * SJ + lj];
+                    const Aux s = aux[lk * SPS + li * SJ + lj];
                     if constexpr (KIND == kFwdPlain64) {
+                        const double xa = min_nonneg(box[c + 1], box[c - 1]);
+                        const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
+                        const double zc = min_nonneg(box[c - PS], box[c + PS]);
                         const double q = eik3_plain(xa, yb, zc, s, A.sp);
-                        box[c] = ref_min(box[c], q);
+                        box[c] = min_nonneg(box[c], q);
                     } else if constexpr (KIND == kFwdFast32) {
-                        const float q = eik3_fast<float>(xa, yb, zc, s, K);
-                        box[c] = ref_min(box[c], q);
-                    } else {   // polish: one Newton step of the local Godunov equation
-                        box[c] = eik3_newton(box[c], xa, yb, zc, s, A.sp);
+                        const float xa = ref_min(box[c + 1], box[c - 1]);
+                        const float yb = ref_min(box[c - HJ], box[c + HJ]);
+                        const float zc = ref_min(box[c - PS], box[c + PS]);
+                        box[c] = ref_min(box[c], eik3_fast(xa, yb, zc, s, A.sp));
+                    } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2)
+                        const double xa = min_nonneg(box[c + 1], box[c - 1]);
+                        const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
+                        const double zc = min_nonneg(box[c - PS], box[c + PS]);
+                        box[c] = eik3_newton(box[c], xa, yb, zc, s, A.slow64, rowbase + gj, A.sp);
                     }
                 }
             } else {
@@ -372,11 +358,11 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                     } else if constexpr (KIND == kAdjFast32) {
                         r = adj3_bulk(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
                                       aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                      box[c - PS], wx32, wy32, wz32);
+                                      box[c - PS], A.sp);
                     } else {
                         r = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
                                         aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                        box[c - PS], box[c], A.sp.inv2[0], A.sp.inv2[1], A.sp.inv2[2]);
+                                        box[c - PS], box[c], A.sp);
                     }
                     box[c] = r;
                 }
@@ -387,22 +373,39 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
 
     // ---- write back; on the last sweep compare with the iteration-start snapshot
     bool changed = false;
-#pragma unroll 4
-    for (int m = 0; m < 32; ++m) {
-        const int rk = m / TI, ri = m % TI;
-        if (rk < ek && ri < ei && lane < ej) {
-            const long long at = (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane;
-            const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
-            fld[at] = v;
-            if (A.last) {
-                const Real p = snp[at];
-                const double diff = fabs((double)p - (double)v);
-                if (diff > A.tol_abs + A.tol_rel * fabs((double)v)) changed = true;
+    if (A.last) {
+#pragma unroll 1
+        for (int m0 = 0; m0 < 32; m0 += 8) {
+            Real p[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int m = m0 + u, rk = m / TI, ri = m % TI;
+                p[u] = Real(0);
+                if (rk < ek && ri < ei && lane < ej) p[u] = snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane];
             }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int m = m0 + u, rk = m / TI, ri = m % TI;
+                if (rk < ek && ri < ei && lane < ej) {
+                    const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+                    fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = v;
+                    if constexpr (sizeof(Real) == 8) {
+                        if (fabs(p[u] - v) > A.tol_abs) changed = true;   // isconv, src/T_pfsm3d.h:126
+                    } else {
+                        if (fabsf(p[u] - v) > A.tol_abs_f + A.tol_rel_f * fabsf(v)) changed = true;
+                    }
+                }
+            }
+        }
+    } else {
+#pragma unroll 4
+        for (int m = 0; m < 32; ++m) {
+            const int rk = m / TI, ri = m % TI;
+            if (rk < ek && ri < ei && lane < ej)
+                fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
         }
     }
     if (A.last && __any_sync(0xffffffffu, changed) && lane == 0) A.changed[inst] = 1;
-    (void)tref;
 }
 
 }  // namespace
@@ -492,11 +495,14 @@ inline unsigned grid_for(long long n) {
 }
 
 __global__ void slowness_kernel(const double* __restrict__ vp, double* __restrict__ s64, float* __restrict__ s32,
-                                long long n) {
+                                double* __restrict__ sq64, int* __restrict__ bad, long long n) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const double s = 1.0 / vp[t];   // s = 1.0/vp, src/T_pfsm3d.h:75
+        const double v = vp[t];
+        if (!(v > 0.0 && v < INFINITY)) *bad = 1;
+        const double s = 1.0 / v;   // s = 1.0/vp, src/T_pfsm3d.h:75
         s64[t] = s;
         if (s32) s32[t] = (float)s;
+        if (sq64) sq64[t] = s * s;
     }
 }
 
@@ -614,8 +620,9 @@ __global__ void gather3_kernel(const double* __restrict__ T, long long fstride, 
         if (e__ != cudaSuccess) return cuda_fail(e__, "kernel launch", __FILE__, __LINE__);    \
     } while (0)
 
-pfast_status launch_slowness(const double* vp, double* s64, float* s32, long long n, cudaStream_t st) {
-    slowness_kernel<<<grid_for(n), kThreads, 0, st>>>(vp, s64, s32, n);
+pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, int* bad, long long n,
+                             cudaStream_t st) {
+    slowness_kernel<<<grid_for(n), kThreads, 0, st>>>(vp, s64, s32, sq64, bad, n);
     PFAST_LAUNCH_CHECK();
     return PFAST_OK;
 }
