@@ -155,22 +155,32 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     a.nbk = dt.nbk;
     a.nbi = dt.nbi;
     a.nbj = dt.nbj;
+    // tile-locking flags: every tile starts unlocked, with no snapshot yet
+    const long long ntiles = (long long)dt.nbk * dt.nbi * dt.nbj;
+    PFAST_TRY(ctx->tflags.ensure(sizeof(int) * 3 * ntiles * nb));
+    a.ntiles = (int)ntiles;
+    a.dirty = ctx->tflags.as<int>();
+    a.stamp = a.dirty + ntiles * nb;
+    a.diff = a.stamp + ntiles * nb;
     cudaStream_t st = ctx->stream;
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0x01, sizeof(int) * ntiles * nb, st));
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * nb, st));
     int it = 0;
     while (!active.empty() && it < maxiter) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
-        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));
+        PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles * nb, st));
+        a.iter = it;
         for (int dir = 0; dir < 8; ++dir) {
             a.dir = dir;
-            a.first = dir == 0;
-            a.last = dir == 7;
             for (int d = 0; d < dt.ndiag; ++d) {
                 PFAST_LAUNCH(ctx, launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
             }
         }
+        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));
+        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.ntiles, a.act, nact, a.changed, st));
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) return cuda_fail(le, "sweep launch", __FILE__, __LINE__);
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
@@ -496,7 +506,7 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
     if (!ctx) return PFAST_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->sq64, &ctx->T32, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
+    for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->sq64, &ctx->T32, &ctx->tflags, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
                       &ctx->ee, &ctx->need, &ctx->misc, &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a,
                       &ctx->f2b, &ctx->f2c})
         b->release();

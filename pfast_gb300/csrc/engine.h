@@ -41,7 +41,7 @@ struct pfast_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     // device work buffers (reused across calls)
-    pfast::DevBuf s64, s32, sq64, T32, T64, L64, scratch, mask, act, changed, ee, need, misc, grad_tmp, vp_tmp, picks_tmp;
+    pfast::DevBuf s64, s32, sq64, T32, tflags, T64, L64, scratch, mask, act, changed, ee, need, misc, grad_tmp, vp_tmp, picks_tmp;
     pfast::DevBuf f2a, f2b, f2c;       // 2D field buffers
     pfast::HostBuf h_act, h_changed, h_ee, h_need;
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;

@@ -29,7 +29,11 @@ struct Sweep3Args {
     int nbk, nbi, nbj;
     Spacing3 sp;
     int dir;                  // sweep order 0..7: bit2 = s3>0 (z), bit1 = s1>0 (rows), bit0 = s2>0 (cols)
-    int first, last;          // first / last sweep of an outer iteration
+    int iter;                 // outer-iteration index (snapshot stamps)
+    int ntiles;               // tiles per instance (nbk*nbi*nbj)
+    int* dirty;               // per (instance, tile): process the tile (see sweep3d_kernel)
+    int* stamp;               // per (instance, tile): iteration of the tile's snapshot
+    int* diff;                // per (instance, tile): differs from its snapshot by > tol
     double tol_abs, tol_rel;  // change test: |new-old| > tol_abs + tol_rel*|new| (FP64 sweeps)
     float tol_abs_f, tol_rel_f;  // the same test for the FP32 sweeps, evaluated in FP32
 };
@@ -47,6 +51,8 @@ pfast_status build_diag_table3(int nz, int nr, int nc, DiagTable3& t);
 void free_diag_table3(DiagTable3& t);
 
 size_t sweep3_smem_bytes(int kind);
+// changed[act[b]] = any diff over the tiles of instance act[b], b < nact.
+pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
 
 // Small 3D kernels.

@@ -19,6 +19,7 @@
 
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 #include "kernels.h"
 
 namespace pfast {
@@ -33,16 +34,21 @@ template <> struct Traits<kAdjPlain64>   { using Real = double; using Aux = doub
 template <> struct Traits<kAdjFast32>    { using Real = float;  using Aux = float;  static constexpr bool adj = true; };
 template <> struct Traits<kAdjPolish64>  { using Real = double; using Aux = double; static constexpr bool adj = true; };
 
-// Shared memory per warp: the field's halo box plus either the slowness tile
-// (forward) or the traveltime halo box (adjoint).
+// Shared memory per warp: the field's halo box, plus the traveltime halo box for
+// the adjoint.  The forward's slowness is read per node through L1 (each lane walks
+// its own row, so a fetched line serves the next steps): keeping it out of shared
+// memory raises the number of resident warps.
 template <int KIND>
 __host__ __device__ constexpr int warp_smem_bytes() {
     using T = Traits<KIND>;
-    return int(HK * PS * sizeof(typename T::Real) +
-               (T::adj ? HK * PS * sizeof(typename T::Aux) : TK * SPS * sizeof(typename T::Aux)));
+    return int(HK * PS * sizeof(typename T::Real) + (T::adj ? HK * PS * sizeof(typename T::Aux) : 0));
 }
 
 __device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
+
+// Polish corrections below this (seconds, or relative for the adjoint) are dropped;
+// two orders of magnitude under the 1e-9 convergence tolerance.
+constexpr float kPolishFloor = 1e-11f;
 
 // ----------------------------------------------------------- node updates
 // Reference Godunov update (src/T_pfsm3d.h:99-119).  a/b/c: neighbour minima along
@@ -124,7 +130,10 @@ __device__ __forceinline__ double eik3_newton(double U0, double a, double b, dou
         const double s = __ldg(slow + node);
         return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
     }
-    return U0 - (double)__fdividef((float)f, fp);
+    const float step = __fdividef((float)f, fp);
+    // corrections far below the 1e-9 convergence tolerance are dropped, so that a
+    // converged region reaches a bitwise fixed point (and its tiles lock)
+    return fabsf(step) <= kPolishFloor ? U0 : U0 - (double)step;
 }
 
 // Adjoint updates.  The reference's upwind formula (src/T_padjoint3d.h:51-66)
@@ -161,9 +170,11 @@ __device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, 
     return 0.0;
 }
 
-// FP32 bulk adjoint update (T as FP32 values; unreached nodes hold INF).
+// FP32 bulk adjoint update (T as FP32 values; unreached nodes hold INF).  A change of
+// less than 2^-24 relative keeps the old value, so converged regions reach a bitwise
+// fixed point (rounding alone would otherwise keep flipping last bits).
 __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float Typ, float Tym, float Tzp, float Tzm,
-                                           float Lxp, float Lxm, float Lyp, float Lym, float Lzp, float Lzm,
+                                           float Lxp, float Lxm, float Lyp, float Lym, float Lzp, float Lzm, float L0,
                                            const Spacing3& sp) {
     const float ti = (float)kInf;
     if (T0 >= ti || Txp >= ti || Txm >= ti || Typ >= ti || Tym >= ti || Tzp >= ti || Tzm >= ti) return 0.f;
@@ -175,7 +186,8 @@ __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float
     e = Tym - T0; den = fmaf(wy, fmaxf(-e, 0.f), den); num = fmaf(wy * fmaxf(e, 0.f), Lym, num);
     e = Tzp - T0; den = fmaf(wz, fmaxf(-e, 0.f), den); num = fmaf(wz * fmaxf(e, 0.f), Lzp, num);
     e = Tzm - T0; den = fmaf(wz, fmaxf(-e, 0.f), den); num = fmaf(wz * fmaxf(e, 0.f), Lzm, num);
-    return (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
+    const float r = (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
+    return fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r;
 }
 
 // FP64 polish adjoint update in residual-correction form: num, den and the residual
@@ -201,51 +213,63 @@ __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm,
     }
     if (!(dbits(den) > dbits(1e-9))) return 0.0;   // den >= 0 by construction
     const double r = fma(-den, L0, num);
-    return L0 + (double)__fdividef((float)r, (float)den);
+    const float step = __fdividef((float)r, (float)den);
+    return fabsf(step) <= kPolishFloor * (1.0f + fabsf((float)L0)) ? L0 : L0 + (double)step;
 }
 
 // ----------------------------------------------------------- tile I/O
 // Load the (TK+2)x(TI+2)x(TJ+2) halo box at origin (k0-1, i0-1, j0-1) into `box`
-// (plane stride PS, row stride HJ).  Out-of-grid entries get `fill`.  Loads are
-// issued 16 per lane before their shared-memory stores, to keep many in flight.
+// (plane stride PS, row stride HJ), one box row per warp instruction (lanes along
+// the row, coalesced); out-of-grid entries get `fill`.  Twelve rows are loaded
+// before they are stored, to keep many loads in flight.
 template <typename T>
 __device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0, int i0, int j0, int nz, int nr,
                                          int nc, T fill, int lane) {
-    constexpr int NE = HK * HI * HJ;
-    constexpr int BATCH = 16;
+    constexpr int NROW = HK * HI;
+    constexpr int RB = 12;
+    static_assert(NROW % RB == 0 && HJ - 32 <= 32, "row batching");
     const long long plane = (long long)nr * nc;
+    const int gj0 = j0 - 1 + lane, gj1 = j0 + 31 + lane;
+    const bool c0 = (unsigned)gj0 < (unsigned)nc;
+    const bool c1 = lane < HJ - 32 && (unsigned)gj1 < (unsigned)nc;
 #pragma unroll 1
-    for (int base = 0; base < NE; base += 32 * BATCH) {
-        T v[BATCH];
+    for (int rb = 0; rb < NROW; rb += RB) {
+        T v0[RB], v1[RB];
 #pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const int e = base + u * 32 + lane;
-            v[u] = fill;
-            if (e < NE) {
-                const int r = e / HJ, x = e - r * HJ;
-                const int z = r / HI, y = r - z * HI;
-                const int gk = k0 - 1 + z, gi = i0 - 1 + y, gj = j0 - 1 + x;
-                if ((unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr && (unsigned)gj < (unsigned)nc)
-                    v[u] = __ldg(g + gk * plane + (long long)gi * nc + gj);
-            }
+        for (int u = 0; u < RB; ++u) {
+            const int r = rb + u, z = r / HI, y = r - z * HI;
+            const int gk = k0 - 1 + z, gi = i0 - 1 + y;
+            const bool rok = (unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr;
+            const T* row = g + gk * plane + (long long)gi * nc;
+            v0[u] = (rok && c0) ? __ldg(row + gj0) : fill;
+            v1[u] = (rok && c1) ? __ldg(row + gj1) : fill;
         }
 #pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const int e = base + u * 32 + lane;
-            if (e < NE) {
-                const int r = e / HJ, x = e - r * HJ;
-                const int z = r / HI, y = r - z * HI;
-                box[z * PS + y * HJ + x] = v[u];
-            }
+        for (int u = 0; u < RB; ++u) {
+            const int r = rb + u, z = r / HI, y = r - z * HI;
+            T* brow = box + z * PS + y * HJ;
+            brow[lane] = v0[u];
+            if (lane < HJ - 32) brow[32 + lane] = v1[u];
         }
     }
 }
 
 // ----------------------------------------------------------- the sweep kernel
+// Tile locking: a tile whose last processing changed no bit of its field, and none
+// of whose face neighbours has changed a face node since, is a fixed point of the
+// node update in every sweep order (each node's update returned its own value
+// with the neighbour values it still has), so it is skipped.  Per (source, tile):
+//   dirty[t]  set by the tile itself or a face neighbour when a node changes,
+//   stamp[t]  outer iteration in which the tile last took its snapshot,
+//   diff[t]   whether the tile differs from its snapshot by more than the
+//             tolerance after its latest processing (cleared each iteration).
+// The outer-iteration test of the reference (isconv) is the OR of diff over the
+// tiles of a source: a skipped tile has not moved.
 template <int KIND>
 __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args A, const int d) {
     using Real = typename Traits<KIND>::Real;
     using Aux = typename Traits<KIND>::Aux;
+    using Bits = typename std::conditional<sizeof(Real) == 8, unsigned long long, unsigned>::type;
     constexpr bool ADJ = Traits<KIND>::adj;
     extern __shared__ __align__(16) unsigned char smem_raw[];
 
@@ -262,6 +286,12 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const int tk = pz ? bkf : A.nbk - 1 - bkf;
     const int ti = py ? bif : A.nbi - 1 - bif;
     const int tj = px ? bjf : A.nbj - 1 - bjf;
+    const int tid = (tk * A.nbi + ti) * A.nbj + tj;
+    int* dirty = A.dirty + (long long)inst * A.ntiles;
+    if (!dirty[tid]) return;   // locked tile (warp-uniform)
+    __syncwarp();
+    if (lane == 0) dirty[tid] = 0;   // face neighbours run in other launches: no race
+
     const int k0 = tk * TK, i0 = ti * TI, j0 = tj * TJ;
     const int ek = min(TK, A.nz - k0), ei = min(TI, A.nr - i0), ej = min(TJ, A.nc - j0);
     const int nz = A.nz, nr = A.nr, nc = A.nc;
@@ -283,24 +313,17 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const bool lane_ok = lkf < ek && lif < ei;
     const int lk = pz ? lkf : ek - 1 - lkf;
     const int li = py ? lif : ei - 1 - lif;
-    if constexpr (!ADJ) {
-        // slowness (or its square) tile [lk][li][lj], rows loaded coalesced, 8 rows in flight
-        const Aux* s = reinterpret_cast<const Aux*>(A.aux);
-#pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
-            const int rk = m / TI, ri = m % TI;
-            if (rk < ek && ri < ei && lane < ej)
-                aux[rk * SPS + ri * SJ + lane] = __ldg(s + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane);
-        }
-    } else {
+    if constexpr (ADJ) {
         const Aux* T = reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride;
         load_box<Aux>(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane);
         if (lane_ok)
             fixed_bits = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
     }
 
-    // ---- snapshot of the iteration start (first sweep of an outer iteration)
-    if (A.first) {
+    // ---- snapshot at the tile's first processing in this outer iteration (its values are
+    // still the iteration-start values then: only the tile itself writes them)
+    int* stamp = A.stamp + (long long)inst * A.ntiles;
+    if (stamp[tid] != A.iter) {
 #pragma unroll 4
         for (int m = 0; m < 32; ++m) {
             const int rk = m / TI, ri = m % TI;
@@ -308,6 +331,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                 snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
                     box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
         }
+        if (lane == 0) stamp[tid] = A.iter;
     }
     __syncwarp();
 
@@ -319,6 +343,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     if constexpr (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
     const bool row_interior = ADJ ? (gk >= 1 && gk <= nz - 2 && gi >= 1 && gi <= nr - 2) : true;
     const long long rowbase = gk * plane + (long long)gi * nc;
+    bool chg = false, chg_jlo = false, chg_jhi = false;   // this lane's pencil changed (anywhere / at lj = 0 / at ej-1)
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
@@ -327,85 +352,117 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
             const int lj = px ? ljf : ej - 1 - ljf;
             const int c = cbase + lj;
             const int gj = j0 + lj;
+            const Real old = box[c];
+            Real nv = old;
             if constexpr (!ADJ) {
                 if (!(gk == sk && gi == si && gj == sj)) {
-                    const Aux s = aux[lk * SPS + li * SJ + lj];
+                    const Aux s = __ldg(reinterpret_cast<const Aux*>(A.aux) + rowbase + gj);
                     if constexpr (KIND == kFwdPlain64) {
                         const double xa = min_nonneg(box[c + 1], box[c - 1]);
                         const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
                         const double zc = min_nonneg(box[c - PS], box[c + PS]);
-                        const double q = eik3_plain(xa, yb, zc, s, A.sp);
-                        box[c] = min_nonneg(box[c], q);
+                        nv = min_nonneg(old, eik3_plain(xa, yb, zc, s, A.sp));
                     } else if constexpr (KIND == kFwdFast32) {
                         const float xa = ref_min(box[c + 1], box[c - 1]);
                         const float yb = ref_min(box[c - HJ], box[c + HJ]);
                         const float zc = ref_min(box[c - PS], box[c + PS]);
-                        box[c] = ref_min(box[c], eik3_fast(xa, yb, zc, s, A.sp));
+                        nv = ref_min(old, eik3_fast(xa, yb, zc, s, A.sp));
                     } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2)
                         const double xa = min_nonneg(box[c + 1], box[c - 1]);
                         const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
                         const double zc = min_nonneg(box[c - PS], box[c + PS]);
-                        box[c] = eik3_newton(box[c], xa, yb, zc, s, A.slow64, rowbase + gj, A.sp);
+                        nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp);
                     }
                 }
             } else {
                 if (row_interior && gj >= 1 && gj <= nc - 2 && !((fixed_bits >> lj) & 1u)) {
-                    Real r;
                     if constexpr (KIND == kAdjPlain64) {
-                        r = adj3_plain(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                       aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                       box[c - PS], A.sp);
-                    } else if constexpr (KIND == kAdjFast32) {
-                        r = adj3_bulk(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                      aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                      box[c - PS], A.sp);
-                    } else {
-                        r = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                        nv = adj3_plain(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
                                         aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                        box[c - PS], box[c], A.sp);
+                                        box[c - PS], A.sp);
+                    } else if constexpr (KIND == kAdjFast32) {
+                        nv = adj3_bulk(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                       aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
+                                       box[c - PS], old, A.sp);
+                    } else {
+                        nv = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                         aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
+                                         box[c - PS], old, A.sp);
                     }
-                    box[c] = r;
                 }
+            }
+            Bits bo, bn;
+            memcpy(&bo, &old, sizeof(Real));
+            memcpy(&bn, &nv, sizeof(Real));
+            if (bo != bn) {
+                box[c] = nv;
+                chg = true;
+                if (lj == 0) chg_jlo = true;
+                if (lj == ej - 1) chg_jhi = true;
             }
         }
         __syncwarp();
     }
 
-    // ---- write back; on the last sweep compare with the iteration-start snapshot
-    bool changed = false;
-    if (A.last) {
+    // ---- nothing changed: the field and its snapshot comparison stand as they are
+    if (!__any_sync(0xffffffffu, chg)) return;
+
+    // ---- unlock this tile and every face neighbour that sees a changed face node
+    const unsigned f_klo = __ballot_sync(0xffffffffu, chg && lk == 0);
+    const unsigned f_khi = __ballot_sync(0xffffffffu, chg && lk == ek - 1);
+    const unsigned f_ilo = __ballot_sync(0xffffffffu, chg && li == 0);
+    const unsigned f_ihi = __ballot_sync(0xffffffffu, chg && li == ei - 1);
+    const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
+    const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
+    if (lane == 0) {
+        const int sk_ = A.nbi * A.nbj;
+        dirty[tid] = 1;
+        if (f_klo && tk > 0) dirty[tid - sk_] = 1;
+        if (f_khi && tk < A.nbk - 1) dirty[tid + sk_] = 1;
+        if (f_ilo && ti > 0) dirty[tid - A.nbj] = 1;
+        if (f_ihi && ti < A.nbi - 1) dirty[tid + A.nbj] = 1;
+        if (f_jlo && tj > 0) dirty[tid - 1] = 1;
+        if (f_jhi && tj < A.nbj - 1) dirty[tid + 1] = 1;
+    }
+
+    // ---- write back and compare with the iteration-start snapshot
+    bool moved = false;
 #pragma unroll 1
-        for (int m0 = 0; m0 < 32; m0 += 8) {
-            Real p[8];
+    for (int m0 = 0; m0 < 32; m0 += 8) {
+        Real p[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int m = m0 + u, rk = m / TI, ri = m % TI;
-                p[u] = Real(0);
-                if (rk < ek && ri < ei && lane < ej) p[u] = snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane];
-            }
+        for (int u = 0; u < 8; ++u) {
+            const int m = m0 + u, rk = m / TI, ri = m % TI;
+            p[u] = Real(0);
+            if (rk < ek && ri < ei && lane < ej) p[u] = snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane];
+        }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int m = m0 + u, rk = m / TI, ri = m % TI;
-                if (rk < ek && ri < ei && lane < ej) {
-                    const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
-                    fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = v;
-                    if constexpr (sizeof(Real) == 8) {
-                        if (fabs(p[u] - v) > A.tol_abs) changed = true;   // isconv, src/T_pfsm3d.h:126
-                    } else {
-                        if (fabsf(p[u] - v) > A.tol_abs_f + A.tol_rel_f * fabsf(v)) changed = true;
-                    }
+        for (int u = 0; u < 8; ++u) {
+            const int m = m0 + u, rk = m / TI, ri = m % TI;
+            if (rk < ek && ri < ei && lane < ej) {
+                const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+                fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = v;
+                if constexpr (sizeof(Real) == 8) {
+                    if (fabs(p[u] - v) > A.tol_abs) moved = true;   // isconv, src/T_pfsm3d.h:126
+                } else {
+                    if (fabsf(p[u] - v) > A.tol_abs_f + A.tol_rel_f * fabsf(v)) moved = true;
                 }
             }
         }
-    } else {
-#pragma unroll 4
-        for (int m = 0; m < 32; ++m) {
-            const int rk = m / TI, ri = m % TI;
-            if (rk < ek && ri < ei && lane < ej)
-                fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
-        }
     }
-    if (A.last && __any_sync(0xffffffffu, changed) && lane == 0) A.changed[inst] = 1;
+    const bool any_moved = __any_sync(0xffffffffu, moved);
+    if (lane == 0) A.diff[(long long)inst * A.ntiles + tid] = any_moved ? 1 : 0;
+}
+
+// changed[act[b]] = OR over the tiles of instance act[b] of diff.
+__global__ void reduce_diff_kernel(const int* __restrict__ diff, int ntiles, const int* __restrict__ act,
+                                   int* __restrict__ changed) {
+    const int inst = act[blockIdx.x];
+    const int* d = diff + (long long)inst * ntiles;
+    int any = 0;
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) any |= d[t];
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) changed[inst] = any ? 1 : 0;
 }
 
 }  // namespace
@@ -467,6 +524,14 @@ static pfast_status launch_one(const Sweep3Args& a, int d, int tiles, int nact, 
     }
     dim3 grid((tiles + kWarps3 - 1) / kWarps3, nact);
     sweep3d_kernel<KIND><<<grid, kWarps3 * 32, smem, st>>>(a, d);
+    return PFAST_OK;
+}
+
+pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st) {
+    if (nact <= 0) return PFAST_OK;
+    reduce_diff_kernel<<<nact, 256, 0, st>>>(diff, ntiles, act, changed);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "reduce_diff launch", __FILE__, __LINE__);
     return PFAST_OK;
 }
 

@@ -11,7 +11,8 @@
 // which each GPU that loads the library holds until the process exits.
 //
 // The array holds, for at most PFAST_NOALLOC_MAX_NODES grid nodes: the slowness
-// field, the iteration-start snapshot, the tile-diagonal table and a few flags.
+// field, the iteration-start snapshot, the tile-diagonal table, the per-tile
+// locking flags and a few words.
 // Its device address is taken with cudaGetSymbolAddress once per device, on the
 // first call made on that device (with that device current); that first call
 // should therefore come before any stream capture.  Every call shares the array
@@ -40,7 +41,8 @@ constexpr size_t kOffSlow = 0;                                              // d
 constexpr size_t kOffSnap = align256(kOffSlow + 8 * (size_t)kMaxNodes);     // double[kMaxNodes]
 constexpr size_t kOffTiles = align256(kOffSnap + 8 * (size_t)kMaxNodes);    // unsigned[kMaxTiles]
 constexpr size_t kOffDiag = align256(kOffTiles + 4 * (size_t)kMaxTiles);    // int[kMaxDiag + 1]
-constexpr size_t kOffWords = align256(kOffDiag + 4 * (size_t)(kMaxDiag + 1));
+constexpr size_t kOffFlags = align256(kOffDiag + 4 * (size_t)(kMaxDiag + 1));   // int[3*kMaxTiles]: dirty, stamp, diff
+constexpr size_t kOffWords = align256(kOffFlags + 12 * (size_t)kMaxTiles);
 // words: [0..1] source linear index (long long), [2..4] source (k,i,j), [5] active id,
 //        [6] changed flag, [7] bad-velocity flag
 constexpr size_t kScratchBytes = align256(kOffWords + 64);
@@ -126,6 +128,8 @@ extern "C" pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src
     int* d_act = words + 5;
     int* d_changed = words + 6;
     int* d_bad = words + 7;
+    int* d_dirty = reinterpret_cast<int*>(base + kOffFlags);
+    const int ntiles = nbk * nbi * nbj;
 
     int hw[8];
     const long long lin = (long long)src_z * nrows * ncols + (long long)src_row * ncols + src_col;
@@ -176,18 +180,26 @@ extern "C" pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src
         a.sp.inv2[k] = 1.0 / dd[k] / dd[k];
     }
     a.tol_abs = kConvTol;
+    a.ntiles = ntiles;
+    a.dirty = d_dirty;
+    a.stamp = d_dirty + ntiles;
+    a.diff = d_dirty + 2 * ntiles;
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0x01, sizeof(int) * ntiles, s));
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles, s));
     // outer iterations of src/T_pfsm3d.h:152: snapshot + 8 sweeps while some node moved by > 1e-9
     for (int it = 0; it < MAXSwp; ++it) {
-        PFAST_CUDA_TRY(cudaMemsetAsync(d_changed, 0, sizeof(int), s));
+        PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles, s));
+        a.iter = it;
         for (int dir = 0; dir < 8; ++dir) {
             a.dir = dir;
-            a.first = dir == 0;
-            a.last = dir == 7;
             for (int d = 0; d < ndiag; ++d) {
                 r = launch_sweep3(kFwdPlain64, a, d, off[d + 1] - off[d], 1, s);
                 if (r) return r;
             }
         }
+        PFAST_CUDA_TRY(cudaMemsetAsync(d_changed, 0, sizeof(int), s));
+        r = launch_reduce_diff(a.diff, ntiles, d_act, 1, d_changed, s);
+        if (r) return r;
         int changed = 0;
         PFAST_CUDA_TRY(cudaMemcpyAsync(&changed, d_changed, sizeof(int), cudaMemcpyDeviceToHost, s));
         PFAST_CUDA_TRY(cudaStreamSynchronize(s));
