@@ -288,6 +288,8 @@ def main():
                 "mixed_over_plain": value / world / plain_value,
                 "accuracy": {"tt_max_rel": tt_max_rel, "grad_rel_l2": grad_rel_l2, "vs": "plain FP64 (bit-identical to the oracle)",
                              "sample_sources": nps},
+                "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                               "of": "one 256-source misfit+gradient evaluation, device-resident"},
                 "misfit": misfit,
                 "step_ms": step_ms,
                 "phase_ms": {k: st[k] for k in ("ms_fwd32", "ms_fwd64", "ms_adj32", "ms_adj64", "ms_other", "ms_total")},
