@@ -146,6 +146,18 @@ pfast_status pfast_survey2d_eval(pfast_ctx* ctx, pfast_survey2d* sv, const doubl
                                  const pfast_options* opt, double* gT, double* gR, double* gRT, double* Et,
                                  double* Er, pfast_stats* stats);
 
+/* One-call host-buffer forms of the 2D survey (copies in and out inside the call);
+ * arguments as in pfast_survey2d_create.  Tr[nrec*(NumofR+1)] (src/RT_PFAST2D.cpp:832-852). */
+pfast_status pfast_forward2d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, double dx, double dz, int nsrc,
+                             const int* src, const int* srnum, int nrec, const int* rec, int NumofR, const double* Z,
+                             const pfast_options* opt, double* Tr, pfast_stats* stats);
+/* Joint gradient with host buffers (src/RT_PFAST2D.cpp:420-457); WR, gT, gR, gRT: [nrows*ncols]. */
+pfast_status pfast_eval2d(pfast_ctx* ctx, const double* vp, const double* WR, int nrows, int ncols, double dx,
+                          double dz, int nsrc, const int* src, const int* srnum, int nrec, const int* rec,
+                          const double* nxy, const double* TT_obs, int NumofR, const double* TR_obs, const double* Z,
+                          const pfast_options* opt, double* gT, double* gR, double* gRT, double* Et, double* Er,
+                          pfast_stats* stats);
+
 /* ------------------------------------------------------- no-allocation entry point
  * No counterpart in the reference.  The traveltime field of one point source --
  * the computation of pfast_fsm3d (plain FP64, bit-identical to it) -- for callers

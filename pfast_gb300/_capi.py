@@ -69,6 +69,9 @@ SIGNATURES = [
     ("pfast_survey2d_forward", _i, [_p, _p, _p, _p, _p, _p]),
     ("pfast_survey2d_eval", _i, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     ("pfast_fsm3d_noalloc", _i, [_p, _p, _i, _i, _i, _i, _d, _d, _d, _i, _i, _i, _p]),
+    ("pfast_forward2d", _i, [_p, _p, _i, _i, _d, _d, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p]),
+    ("pfast_eval2d", _i, [_p, _p, _p, _i, _i, _d, _d, _i, _p, _p, _i, _p, _p, _p, _i, _p, _p, _p, _p, _p, _p, _p, _p,
+                          _p]),
 ]
 PFAST_NOALLOC_MAX_NODES = 1048576
 

@@ -65,7 +65,40 @@ def build(verbose=False, force=False):
                 print(err)
     if force or jobs or _stale(LIB, objs):
         run([cc] + ARCH + ["-shared", "-o", LIB] + objs)
+    build_drivers(verbose=verbose, force=force)
     return LIB
+
+
+# Drop-in executables: (binary name, source, extra defines)
+DRIVERS = [("T_PFAST3D_FW", "t_pfast3d_fw.cpp", []),
+           ("RT_PFAST2D_FW", "rt_pfast2d_fw.cpp", []),
+           ("RT_PFAST2D_FW_NoS", "rt_pfast2d_fw.cpp", ["-DNoShotGather"])]
+BINDIR = os.path.join(HERE, "bin")
+
+
+def build_drivers(verbose=False, force=False):
+    os.makedirs(BINDIR, exist_ok=True)
+    ddir = os.path.join(HERE, "drivers")
+    inc = os.path.join(HERE, "..", "include")
+    jobs = []
+    for name, src, defs in DRIVERS:
+        out = os.path.join(BINDIR, name)
+        deps = [os.path.join(ddir, src), os.path.join(ddir, "driver_io.h"), LIB]
+        if force or _stale(out, deps):
+            jobs.append(["g++", "-O2", "-std=c++17", "-I", inc] + defs +
+                        [os.path.join(ddir, src), "-o", out, "-L", LIBDIR, "-lpfast_gb300",
+                         "-Wl,-rpath,$ORIGIN/../lib"])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+    with ThreadPoolExecutor(max(1, len(jobs))) as ex:
+        list(ex.map(run, jobs))
+    return BINDIR
 
 
 if __name__ == "__main__":

@@ -869,3 +869,87 @@ pfast_status pfast_Radjoint_fsm2d(double* UR, double* Td, double* Tu, double* TR
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ host-buffer forms
+namespace {
+
+struct HostDev2 {
+    pfast_ctx* ctx;
+    std::vector<void*> ptrs;
+    ~HostDev2() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    pfast_status up(double** d, const double* h, size_t n) {
+        void* p = nullptr;
+        PFAST_CUDA_TRY(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1)));
+        ptrs.push_back(p);
+        if (h) PFAST_CUDA_TRY(cudaMemcpyAsync(p, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        *d = static_cast<double*>(p);
+        return PFAST_OK;
+    }
+};
+
+pfast_status down(pfast_ctx* ctx, double* h, const double* d, size_t n) {
+    PFAST_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return PFAST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pfast_status pfast_forward2d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, double dx, double dz, int nsrc,
+                             const int* src, const int* srnum, int nrec, const int* rec, int NumofR, const double* Z,
+                             const pfast_options* opt, double* Tr, pfast_stats* stats) {
+    if (!ctx || !vp || !Tr) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
+    pfast_survey2d* sv = nullptr;
+    PFAST_TRY2(pfast_survey2d_create(ctx, nrows, ncols, dx, dz, nsrc, src, srnum, nrec, rec, nullptr, nullptr, NumofR,
+                                     nullptr, Z, &sv));
+    const size_t N = (size_t)nrows * ncols;
+    HostDev2 hd{ctx, {}};
+    double *d_vp = nullptr, *d_tr = nullptr;
+    pfast_status r = hd.up(&d_vp, vp, N);
+    if (!r) r = hd.up(&d_tr, nullptr, (size_t)std::max(nrec, 1) * (NumofR + 1));
+    if (!r) r = pfast_survey2d_forward(ctx, sv, d_vp, opt, d_tr, stats);
+    if (!r && nrec > 0) r = down(ctx, Tr, d_tr, (size_t)nrec * (NumofR + 1));
+    if (!r) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "synchronize", __FILE__, __LINE__);
+    }
+    pfast_survey2d_destroy(sv);
+    return r;
+}
+
+pfast_status pfast_eval2d(pfast_ctx* ctx, const double* vp, const double* WR, int nrows, int ncols, double dx,
+                          double dz, int nsrc, const int* src, const int* srnum, int nrec, const int* rec,
+                          const double* nxy, const double* TT_obs, int NumofR, const double* TR_obs, const double* Z,
+                          const pfast_options* opt, double* gT, double* gR, double* gRT, double* Et, double* Er,
+                          pfast_stats* stats) {
+    if (!ctx || !vp || !WR || !gT || !gR || !gRT || !nxy || !TT_obs) {
+        set_last_error("null argument");
+        return PFAST_ERR_INVALID;
+    }
+    pfast_survey2d* sv = nullptr;
+    PFAST_TRY2(pfast_survey2d_create(ctx, nrows, ncols, dx, dz, nsrc, src, srnum, nrec, rec, nxy, TT_obs, NumofR,
+                                     TR_obs, Z, &sv));
+    const size_t N = (size_t)nrows * ncols;
+    HostDev2 hd{ctx, {}};
+    double *d_vp = nullptr, *d_wr = nullptr, *d_gt = nullptr, *d_gr = nullptr, *d_grt = nullptr;
+    pfast_status r = hd.up(&d_vp, vp, N);
+    if (!r) r = hd.up(&d_wr, WR, N);
+    if (!r) r = hd.up(&d_gt, nullptr, N);
+    if (!r) r = hd.up(&d_gr, nullptr, N);
+    if (!r) r = hd.up(&d_grt, nullptr, N);
+    if (!r) r = pfast_survey2d_eval(ctx, sv, d_vp, d_wr, opt, d_gt, d_gr, d_grt, Et, Er, stats);
+    if (!r) r = down(ctx, gT, d_gt, N);
+    if (!r) r = down(ctx, gR, d_gr, N);
+    if (!r) r = down(ctx, gRT, d_grt, N);
+    if (!r) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "synchronize", __FILE__, __LINE__);
+    }
+    pfast_survey2d_destroy(sv);
+    return r;
+}
+
+}  // extern "C"
