@@ -31,6 +31,8 @@ typedef int pfast_status;
 #define PFAST_ERR_NO_DEVICE 4            /* no usable CUDA device */
 #define PFAST_ERR_NO_REFLECTION_POINT 5  /* no node above a reflector (src/RT_pfsm2d.h:232,257,281) */
 #define PFAST_ERR_NEGATIVE_TIME 6        /* reflected time < 0 (src/RT_pfsm2d.h:225-227,253,274) */
+#define PFAST_ERR_OVER_CORRECTED 7       /* check_conv: sqrt(max (a*dk/vp)^2) / N >= 1 (src/RT_padjoint2d.h:489-490) */
+#define PFAST_ERR_LINE_SEARCH 8          /* cubicInterp has no value for its arguments (src/RT_padjoint2d.h:619-630) */
 
 /* Arithmetic of the sweeps. */
 #define PFAST_PLAIN_FP64 0   /* reference arithmetic in FP64, bit-identical with FMA contraction off */
@@ -157,6 +159,96 @@ pfast_status pfast_eval2d(pfast_ctx* ctx, const double* vp, const double* WR, in
                           const double* nxy, const double* TT_obs, int NumofR, const double* TR_obs, const double* Z,
                           const pfast_options* opt, double* gT, double* gR, double* gRT, double* Et, double* Er,
                           pfast_stats* stats);
+
+/* ------------------------------------------------------------------ inversion loop
+ * The drivers' outer loop (src/RT_PFAST2D.cpp:412-816, src/T_PFAST3D.cpp:359-656) with
+ * every N-vector resident on the device: gradient of the survey, FFT low-pass
+ * regularisation (regu2d / regu3d), search direction (L-BFGS two-loop recursion, HS or
+ * CG_DESCENT), line search, updatevp and check_conv.  One pfast_inversion_step is one
+ * "Iterating No. k" of the reference; the report carries what the reference prints.
+ * Inner products are summed in a fixed order (identical results run to run); the FFT is
+ * cuFFT's, so results agree with the reference to rounding, not bit for bit.
+ */
+typedef struct pfast_inversion pfast_inversion;
+
+#define PFAST_SCHEME_HS 1          /* beta_HS, src/RT_padjoint2d.h:560-571 */
+#define PFAST_SCHEME_CGDESCENT 2   /* beta_CGDESCENT, src/RT_padjoint2d.h:573-588 */
+#define PFAST_SCHEME_LBFGS 3       /* gd2sk + two-loop recursion, src/RT_PFAST2D.cpp:520-546 */
+#define PFAST_LS_NONE 0            /* lsrc 0: step alpha1 as is */
+#define PFAST_LS_SECANT_EXACT 1    /* lsrc 1: secant on the directional derivative */
+#define PFAST_LS_SECANT_WOLFE 2    /* lsrc 2: secant with the strong Wolfe test */
+#define PFAST_LS_CUBIC 3           /* lsrc 3: cubic interpolation (strong Wolfe loop with L-BFGS) */
+#define PFAST_RT_TRANSMISSION 1    /* RTtag (2D): gradient and line-search misfit of transmission only */
+#define PFAST_RT_REFLECTION 2      /*              reflection only */
+#define PFAST_RT_JOINT 3           /*              gT*(1-WR) + gR*WR and Et + Er */
+
+typedef struct {
+    pfast_options eval;   /* gradient evaluations (precision, MAXSwp, batch cap) */
+    int schemetag;        /* PFAST_SCHEME_*; 3D runs L-BFGS whatever is asked (src/T_PFAST3D.cpp:428) */
+    int lsrc;             /* PFAST_LS_* */
+    int LM;               /* L-BFGS memory (drivers' command-line argument, default 5) */
+    int max_linesearch;   /* MAXLineSch: trial models per line search (2D 5, 3D 2); at most 16 */
+    int rttag;            /* PFAST_RT_* (2D) */
+    double nux, nuy, nuz; /* regularisation lengths.  2D: nux (columns, dx) and nuz (rows, dz) are
+                             the .inp's two values, which the 2D driver calls nux, nuy */
+    double minv, maxv;    /* updatevp clamp, MINV / MAXV: 1600 / 4500 (2D), 1400 / 8000 (3D) */
+    double conv_tol;      /* check_conv stops when (E[k-1]-E[k])/E[k-1] <= conv_tol: 1e-3 (2D), 1e-2 (3D) */
+    int keep_components;  /* 2D: also regularise gR and gT each iteration (the driver writes them) */
+} pfast_invert_options;
+
+#define PFAST_INV_MAX_TRIALS 16
+typedef struct {
+    int iter;             /* Iterk, from 1 */
+    double E, Et, Er;     /* misfits at the iteration's starting model: global_E (Et + Er in 2D) and parts */
+    double alpha_start;   /* alpha1 entering the line search */
+    int ntrials;          /* rows of trial[] filled (lsrc 2 and 3) */
+    double trial[PFAST_INV_MAX_TRIALS][6];  /* (alpha0, alpha1, phi0, phi1, dphi0, dphi1) as printed */
+    int count;            /* the line search's `count` after its loop */
+    int stopped;          /* 1: count > MAXLineSch ("Line Search Stopped") */
+    double stepsize;      /* alpha1 applied by updatevp */
+    int converged;        /* check_conv returned true */
+    int evals;            /* gradient evaluations made in this iteration */
+    double ms_eval;       /* wall time of those evaluations */
+    double ms_linesearch; /* wall time of the line search, its evaluations included */
+    double ms_total;      /* wall time of the iteration */
+} pfast_invert_report;
+
+/* Fields readable after a step (pfast_inversion_get / _field). */
+#define PFAST_INV_VP 0         /* current model (<p>_<k> after step k) */
+#define PFAST_INV_GRAD_RAW 1   /* step's gradient before regularisation (<p>_bf_regu_RT<k>) */
+#define PFAST_INV_GRAD 2       /* after regularisation (<p>_af_regu_RT<k>) */
+#define PFAST_INV_DIRECTION 3  /* search direction dk */
+#define PFAST_INV_GR_RAW 4     /* 2D with keep_components: reflection gradient, before / after */
+#define PFAST_INV_GR 5
+#define PFAST_INV_GT_RAW 6     /*                          transmission gradient, before / after */
+#define PFAST_INV_GT 7
+
+/* Defaults of the reference drivers for dim 2 (RT_PFAST2D) or 3 (T_PFAST3D). */
+void pfast_invert_default_options(int dim, pfast_invert_options* opt);
+/* vp [nrows*ncols] and WR [nrows*ncols] are HOST arrays (copied).  The survey must hold
+ * picks and outlive the inversion. */
+pfast_status pfast_inversion2d_create(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, const double* WR,
+                                      const pfast_invert_options* opt, pfast_inversion** out);
+/* vp [nz*nrows*ncols]: HOST array (copied). */
+pfast_status pfast_inversion3d_create(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp,
+                                      const pfast_invert_options* opt, pfast_inversion** out);
+/* Resume of T_PFAST3D (src/T_PFAST3D.cpp:346-385): `k` iterations are done and the run stopped
+ * inside iteration k+1 after writing its gradient.  The next step skips its gradient evaluation
+ * and uses grad_cur (<p>_bf_regu_<k+1>.vp, unregularised, used as is) as the gradient,
+ * grad_prev (<p>_bf_regu_<k>.vp) as the previous gradient and search direction, E_hist[0..nE)
+ * (global_E.tmp, nE >= k+1) as the misfit history and alpha1 (alpha1.tmp) as the last step.
+ * The L-BFGS pair store starts empty.  The model is the one given at create (<p>.vp<k>).
+ * HOST arrays [nz*nrows*ncols]. */
+pfast_status pfast_inversion_resume(pfast_inversion* inv, int k, const double* grad_prev, const double* grad_cur,
+                                    const double* E_hist, int nE, double alpha1);
+/* One outer iteration.  Returns PFAST_ERR_OVER_CORRECTED after the model update when check_conv
+ * aborts (the report and the updated model are still readable). */
+pfast_status pfast_inversion_step(pfast_inversion* inv, pfast_invert_report* rep);
+/* Copy a field (PFAST_INV_*) to a HOST array of the model's size. */
+pfast_status pfast_inversion_get(pfast_inversion* inv, int field, double* host);
+/* The DEVICE array of a field (valid until the next step or destroy). */
+pfast_status pfast_inversion_field(pfast_inversion* inv, int field, const double** dev);
+pfast_status pfast_inversion_destroy(pfast_inversion* inv);
 
 /* ------------------------------------------------------- no-allocation entry point
  * No counterpart in the reference.  The traveltime field of one point source --

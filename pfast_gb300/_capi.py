@@ -16,6 +16,8 @@ PFAST_ERR_NOMEM = 3
 PFAST_ERR_NO_DEVICE = 4
 PFAST_ERR_NO_REFLECTION_POINT = 5
 PFAST_ERR_NEGATIVE_TIME = 6
+PFAST_ERR_OVER_CORRECTED = 7
+PFAST_ERR_LINE_SEARCH = 8
 
 PFAST_PLAIN_FP64 = 0
 PFAST_MIXED = 1
@@ -40,6 +42,39 @@ class Stats(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+PFAST_SCHEME_HS, PFAST_SCHEME_CGDESCENT, PFAST_SCHEME_LBFGS = 1, 2, 3
+PFAST_LS_NONE, PFAST_LS_SECANT_EXACT, PFAST_LS_SECANT_WOLFE, PFAST_LS_CUBIC = 0, 1, 2, 3
+PFAST_RT_TRANSMISSION, PFAST_RT_REFLECTION, PFAST_RT_JOINT = 1, 2, 3
+PFAST_INV_MAX_TRIALS = 16
+(PFAST_INV_VP, PFAST_INV_GRAD_RAW, PFAST_INV_GRAD, PFAST_INV_DIRECTION, PFAST_INV_GR_RAW, PFAST_INV_GR,
+ PFAST_INV_GT_RAW, PFAST_INV_GT) = range(8)
+
+
+class InvertOptions(C.Structure):
+    _fields_ = [
+        ("eval", Options), ("schemetag", C.c_int), ("lsrc", C.c_int), ("LM", C.c_int),
+        ("max_linesearch", C.c_int), ("rttag", C.c_int),
+        ("nux", C.c_double), ("nuy", C.c_double), ("nuz", C.c_double),
+        ("minv", C.c_double), ("maxv", C.c_double), ("conv_tol", C.c_double),
+        ("keep_components", C.c_int),
+    ]
+
+
+class InvertReport(C.Structure):
+    _fields_ = [
+        ("iter", C.c_int), ("E", C.c_double), ("Et", C.c_double), ("Er", C.c_double),
+        ("alpha_start", C.c_double), ("ntrials", C.c_int),
+        ("trial", (C.c_double * 6) * PFAST_INV_MAX_TRIALS),
+        ("count", C.c_int), ("stopped", C.c_int), ("stepsize", C.c_double), ("converged", C.c_int),
+        ("evals", C.c_int), ("ms_eval", C.c_double), ("ms_linesearch", C.c_double), ("ms_total", C.c_double),
+    ]
+
+    def as_dict(self):
+        d = {name: getattr(self, name) for name, _ in self._fields_ if name != "trial"}
+        d["trials"] = [tuple(self.trial[k]) for k in range(self.ntrials)]
+        return d
 
 
 # (name, restype, argtypes) of every entry point in include/pfast_gb300.h
@@ -72,6 +107,14 @@ SIGNATURES = [
     ("pfast_forward2d", _i, [_p, _p, _i, _i, _d, _d, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p]),
     ("pfast_eval2d", _i, [_p, _p, _p, _i, _i, _d, _d, _i, _p, _p, _i, _p, _p, _p, _i, _p, _p, _p, _p, _p, _p, _p, _p,
                           _p]),
+    ("pfast_invert_default_options", None, [_i, _p]),
+    ("pfast_inversion2d_create", _i, [_p, _p, _p, _p, _p, _p]),
+    ("pfast_inversion3d_create", _i, [_p, _p, _p, _p, _p]),
+    ("pfast_inversion_resume", _i, [_p, _i, _p, _p, _p, _i, _d]),
+    ("pfast_inversion_step", _i, [_p, _p]),
+    ("pfast_inversion_get", _i, [_p, _i, _p]),
+    ("pfast_inversion_field", _i, [_p, _i, _p]),
+    ("pfast_inversion_destroy", _i, [_p]),
 ]
 PFAST_NOALLOC_MAX_NODES = 1048576
 

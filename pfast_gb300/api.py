@@ -10,6 +10,8 @@ Two layers, both over the C ABI (include/pfast_gb300.h):
   PfastError.  The adjoint functions return the misfit EE, as the reference does.
 * Batched surveys (Survey3D / Survey2D): geometry and picks resident on the GPU,
   all sources of an evaluation in one call, device tensors in and out.
+* Inversion: the drivers' outer loop (src/RT_PFAST2D.cpp:412-816,
+  src/T_PFAST3D.cpp:359-656) over a survey, one call per "Iterating No. k".
 """
 import ctypes as C
 
@@ -19,7 +21,8 @@ from . import _capi
 from ._capi import PFAST_MIXED, PFAST_PLAIN_FP64, PfastError, check, lib
 
 __all__ = ["fsm3d", "adjoint_fsm3d", "RT_fsm2d", "Tadjoint_fsm2d", "Radjoint_fsm2d", "Context", "Survey3D",
-           "Survey2D", "eval3d_host", "forward3d_host", "PfastError", "PFAST_PLAIN_FP64", "PFAST_MIXED"]
+           "Survey2D", "eval3d_host", "forward3d_host", "Inversion", "invert_options", "PfastError", "PFAST_PLAIN_FP64",
+           "PFAST_MIXED"]
 
 
 def _arr(a, dtype, name, writable=False):
@@ -299,3 +302,98 @@ def forward3d_host(ctx, vp, dx, dy, dz, src, srnum, rec, precision=PFAST_PLAIN_F
                                 src.ctypes.data, srnum.ctypes.data, rec.ctypes.data, C.byref(o), picks.ctypes.data,
                                 C.byref(st)), "forward3d")
     return picks[:int(srnum.sum())], st.as_dict()
+
+
+# ------------------------------------------------------------ inversion loop
+def invert_options(dim, **kw):
+    """pfast_invert_options with the reference driver's defaults for `dim` (2 or 3), overridden by
+    keywords: precision, maxswp, max_batch (gradient evaluations), schemetag, lsrc, LM,
+    max_linesearch, rttag, nux, nuy, nuz, minv, maxv, conv_tol, keep_components."""
+    o = _capi.InvertOptions()
+    lib().pfast_invert_default_options(int(dim), C.byref(o))
+    for k, v in kw.items():
+        if k in ("precision", "maxswp", "max_batch"):
+            setattr(o.eval, k, int(v))
+        elif k in dict(_capi.InvertOptions._fields_):
+            setattr(o, k, v)
+        else:
+            raise TypeError(f"unknown inversion option {k!r}")
+    return o
+
+
+class Inversion:
+    """The outer inversion loop on the device (pfast_inversion*).
+
+    Inversion(survey, vp, WR=None, **options): survey is a Survey2D (WR required, float64
+    [nrows, ncols]) or a Survey3D; vp is the starting model as a float64 host array.  step()
+    runs one iteration and returns the report the reference prints (misfits, the line-search
+    rows (alpha0, alpha1, phi0, phi1, dphi0, dphi1), the step size, convergence).  step()
+    raises PfastError with status PFAST_ERR_OVER_CORRECTED where the reference aborts with
+    "Over corrected"; the updated model is still readable."""
+
+    FIELDS = dict(vp=_capi.PFAST_INV_VP, grad_raw=_capi.PFAST_INV_GRAD_RAW, grad=_capi.PFAST_INV_GRAD,
+                  direction=_capi.PFAST_INV_DIRECTION, gR_raw=_capi.PFAST_INV_GR_RAW, gR=_capi.PFAST_INV_GR,
+                  gT_raw=_capi.PFAST_INV_GT_RAW, gT=_capi.PFAST_INV_GT)
+
+    def __init__(self, survey, vp, WR=None, **options):
+        self.survey = survey
+        self.ctx = survey.ctx
+        self.shape = tuple(survey.shape)
+        dim = len(self.shape)
+        self.options = invert_options(dim, **options)
+        vp = np.ascontiguousarray(vp, np.float64).reshape(self.shape)
+        self._h = C.c_void_p()
+        if dim == 2:
+            if WR is None:
+                raise ValueError("a 2D inversion needs WR")
+            wr = np.ascontiguousarray(np.broadcast_to(np.asarray(WR, np.float64), self.shape))
+            check(lib().pfast_inversion2d_create(self.ctx.handle, survey._h, vp.ctypes.data, wr.ctypes.data,
+                                                 C.byref(self.options), C.byref(self._h)), "inversion2d_create")
+        else:
+            check(lib().pfast_inversion3d_create(self.ctx.handle, survey._h, vp.ctypes.data, C.byref(self.options),
+                                                 C.byref(self._h)), "inversion3d_create")
+        self.history = []
+
+    def resume(self, k, grad_prev, grad_cur, E_hist, alpha1):
+        """T_PFAST3D's resume: k iterations done, the next step uses grad_cur (unregularised) and
+        grad_prev, the misfit history E_hist and the last step length alpha1."""
+        gp = np.ascontiguousarray(grad_prev, np.float64).reshape(self.shape)
+        gc = np.ascontiguousarray(grad_cur, np.float64).reshape(self.shape)
+        eh = np.ascontiguousarray(E_hist, np.float64)
+        check(lib().pfast_inversion_resume(self._h, int(k), gp.ctypes.data, gc.ctypes.data, eh.ctypes.data, len(eh),
+                                           float(alpha1)), "inversion_resume")
+        self.history = [None] * int(k)
+
+    def step(self):
+        rep = _capi.InvertReport()
+        st = lib().pfast_inversion_step(self._h, C.byref(rep))
+        d = rep.as_dict()
+        self.history.append(d)
+        check(st, "inversion_step")
+        return d
+
+    def run(self, max_iter):
+        """Iterate until check_conv stops the loop or max_iter iterations ran (MAXIter)."""
+        out = []
+        while len(self.history) < max_iter:
+            d = self.step()
+            out.append(d)
+            if d["converged"]:
+                break
+        return out
+
+    def get(self, field="vp"):
+        a = np.empty(self.shape)
+        check(lib().pfast_inversion_get(self._h, self.FIELDS[field], a.ctypes.data), "inversion_get")
+        return a
+
+    def close(self):
+        if self._h:
+            lib().pfast_inversion_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,8 +1,8 @@
 """Build recipe of the pfast_gb300 CUDA library (sm_103a only).
 
 Compiles pfast_gb300/csrc/*.cu in parallel with nvcc and links
-pfast_gb300/lib/libpfast_gb300.so (CUDA runtime linked statically, C ABI in
-include/pfast_gb300.h).  -fmad=false: no FMA contraction anywhere, so the plain
+pfast_gb300/lib/libpfast_gb300.so (CUDA runtime linked statically, cuFFT
+dynamically from the toolkit, C ABI in include/pfast_gb300.h).  -fmad=false: no FMA contraction anywhere, so the plain
 FP64 kernels evaluate the reference's expressions exactly; the fast kernels
 request FMA explicitly with fma().
 """
@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libpfast_gb300.so")
-SOURCES = ["kernels3d.cu", "kernels2d.cu", "engine.cu", "engine2d.cu", "noalloc.cu"]
+SOURCES = ["kernels3d.cu", "kernels2d.cu", "engine.cu", "engine2d.cu", "noalloc.cu", "invert.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"] + ARCH
@@ -27,6 +27,16 @@ def nvcc():
     if not os.path.exists(cand):
         raise RuntimeError("nvcc not found: the CUDA toolkit is required to build pfast_gb300")
     return cand
+
+
+def cuda_libdir():
+    """Directory of the toolkit's shared libraries (libcufft), recorded as the library's rpath."""
+    root = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    for sub in ("lib64", "lib"):
+        d = os.path.join(root, sub)
+        if os.path.exists(os.path.join(d, "libcufft.so")):
+            return d
+    raise RuntimeError("libcufft.so not found under " + root)
 
 
 def _stale(out, deps):
@@ -64,7 +74,9 @@ def build(verbose=False, force=False):
             if verbose and err.strip():
                 print(err)
     if force or jobs or _stale(LIB, objs):
-        run([cc] + ARCH + ["-shared", "-o", LIB] + objs)
+        libdir = cuda_libdir()
+        run([cc] + ARCH + ["-shared", "-o", LIB] + objs +
+            ["-L" + libdir, "-lcufft", "-Xlinker", "-rpath", "-Xlinker", libdir])
     build_drivers(verbose=verbose, force=force)
     return LIB
 
@@ -72,7 +84,9 @@ def build(verbose=False, force=False):
 # Drop-in executables: (binary name, source, extra defines)
 DRIVERS = [("T_PFAST3D_FW", "t_pfast3d_fw.cpp", []),
            ("RT_PFAST2D_FW", "rt_pfast2d_fw.cpp", []),
-           ("RT_PFAST2D_FW_NoS", "rt_pfast2d_fw.cpp", ["-DNoShotGather"])]
+           ("RT_PFAST2D_FW_NoS", "rt_pfast2d_fw.cpp", ["-DNoShotGather"]),
+           ("T_PFAST3D", "t_pfast3d.cpp", []),
+           ("RT_PFAST2D", "rt_pfast2d.cpp", [])]
 BINDIR = os.path.join(HERE, "bin")
 
 

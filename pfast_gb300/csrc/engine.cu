@@ -465,6 +465,8 @@ const char* pfast_status_string(pfast_status s) {
         case PFAST_ERR_NO_DEVICE: return "no CUDA device";
         case PFAST_ERR_NO_REFLECTION_POINT: return "no node above a reflector";
         case PFAST_ERR_NEGATIVE_TIME: return "negative reflected traveltime";
+        case PFAST_ERR_OVER_CORRECTED: return "over corrected: the model update is too large";
+        case PFAST_ERR_LINE_SEARCH: return "line search: cubic interpolation has no minimiser";
     }
     return "unknown status";
 }

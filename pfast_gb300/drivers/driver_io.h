@@ -79,7 +79,74 @@ inline void writemod(const std::string& path, const double* a, size_t count) {
     std::fclose(f);
 }
 
+// writemod with the reference's message (src/RT_pfsm2d.h:49-57)
+inline void writemod_logged(const std::string& path, const double* a, size_t count) {
+    std::printf(" \n...writing file:\n\t %s\n", path.c_str());
+    writemod(path, a, count);
+}
+
+inline std::vector<double> readmod_logged(const std::string& path, size_t count) {
+    std::printf(" \n...reading file:\n\t %s\n", path.c_str());
+    return readmod(path, count);
+}
+
 inline int to_index(double metres, double h) { return (int)std::ceil(metres / h) - 1; }
+
+// The line-search messages of one iteration, as the drivers print them
+// (src/RT_PFAST2D.cpp:561-815, src/T_PFAST3D.cpp:505-645).  `secs`: the search's wall time.
+inline void print_linesearch(const pfast_invert_report& r, int lsrc, int schemetag, int dim) {
+    const double secs = r.ms_linesearch / 1000.0;
+    auto trials = [&]() {
+        for (int t = 0; t < r.ntrials; ++t)
+            std::printf("(alpha0,alpha1,phi0,phi1,dphi0,dphi1)=(%g %g %g %g %g %g\n", r.trial[t][0], r.trial[t][1],
+                        r.trial[t][2], r.trial[t][3], r.trial[t][4], r.trial[t][5]);
+    };
+    auto wolfe_end = [&]() {
+        if (r.stopped)
+            std::printf("Line Search Stopped, takes %g seconds, Stepsize=%f\n ...Updating velocity now...\n", secs,
+                        r.stepsize);
+        else
+            std::printf("Wolfe condition satisfied After %d Iterations, takes %g seconds, Stepsize=%f\n...Updating "
+                        "velocity now...\n", r.count, secs, r.stepsize);
+    };
+    switch (lsrc) {
+        case PFAST_LS_SECANT_EXACT:
+            std::printf("Secant Method Line Search for 'exact' condition (alpha1=%g)...\n", r.alpha_start);
+            if (r.stopped)
+                std::printf("Line Search Stopped, takes %g seconds, Stepsize=%f\n ...Updating velocity now...\n", secs,
+                            r.stepsize);
+            else
+                std::printf("Line Search Completed After %d Iterations, takes %g seconds, Stepsize=%f\n...Updating "
+                            "velocity now...\n", r.count, secs, r.stepsize);
+            break;
+        case PFAST_LS_SECANT_WOLFE:
+            std::printf(dim == 2 ? "Secant Method Line Search with Strong Wolfe Condition (alpha1=%g)...\n"
+                                 : "Secant Method Line Search for Strong Wolfe Condition (alpha1=%g)...\n",
+                        r.alpha_start);
+            trials();
+            wolfe_end();
+            break;
+        case PFAST_LS_CUBIC:
+            if (dim == 3)
+                std::printf("Cubic Interpolation Line Searching (alpha1=%g)...\n", r.alpha_start);
+            else if (schemetag == PFAST_SCHEME_LBFGS)
+                std::printf("Cubic Interpolation Line Search with Strong Wolfe Condition (alpha1=%g)...\n", r.alpha_start);
+            else
+                std::printf("Cubic Interpolation Line Search (alpha1=%g)...\n", r.alpha_start);
+            trials();
+            if (dim == 3 || schemetag == PFAST_SCHEME_LBFGS) wolfe_end();
+            break;
+        default:
+            std::printf("No Line Searching, Stepsize=%f\n", r.stepsize);
+            break;
+    }
+}
+
+// Iteration cap: the drivers' MAXIter unless PFAST_MAXITER is set (a cap for test runs).
+inline int max_iter_from_env(int dflt) {
+    const char* p = std::getenv("PFAST_MAXITER");
+    return (p && std::atoi(p) > 0) ? std::atoi(p) : dflt;
+}
 
 inline std::string prefix_of(const std::string& vp0, int drop = 3) {
     return vp0.size() > (size_t)drop ? vp0.substr(0, vp0.size() - drop) : std::string();

@@ -13,11 +13,16 @@ reference tree; the fixtures are committed so nothing else needs it).
   sources, with the joint gradient and misfits computed by the reference's own
   Tadjoint_fsm2d / Radjoint_fsm2d built into oracle/_ref (SHA-256 of the gradient
   bytes, misfits as exact doubles).
+* rt2d_inv_trace.npz -- the shipped inversion case with all 56 sources: the noisy picks
+  of models/RT_SynMod2D_Inv_rand2p.rec (columns 4-6; geometry = rt2d_fw_golden's) and
+  the lines the reference printed for iterations 1-4 of its three runs
+  (par/RT_SynMod2D_Inv_RT.out, _Trans.out, _Ref.out: RTtag 3, 1, 2): the residual line
+  and the line-search rows, numbers as printed (%g).
 * pins3d.json -- seeded small 3D cases: SHA-256 of the traveltime and adjoint
   fields and the misfit bits produced by the reference's fsm3d / adjoint_fsm3d
   (oracle/_ref).
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [trace]   (trace: only rt2d_inv_trace.npz)
 """
 import hashlib
 import json
@@ -90,7 +95,40 @@ def pins3d():
     return out
 
 
+TRACE_ITERS = 4
+
+
+def trace_lines(path, iters=TRACE_ITERS):
+    """The "Average Time Residual" and "(alpha0,...)" lines of iterations 1..iters of a log."""
+    out, it = [], 0
+    for line in open(path):
+        if line.startswith("Iterating No."):
+            it += 1
+            if it > iters:
+                break
+        elif it and (line.startswith("Average Time Residual") or line.startswith("(alpha0,alpha1")):
+            out.append(line.rstrip("\n"))
+    return out
+
+
+def inversion_trace():
+    noisy = pio.readmod(os.path.join(M, "RT_SynMod2D_Inv_rand2p.rec"), 33600 * 7).reshape(33600, 7)
+    fw_rec = pio.readmod(os.path.join(M, "RT_SynMod2D_FW.rec"), 33600 * 4).reshape(33600, 4)
+    assert np.array_equal(noisy[:, :4], pio.readmod(os.path.join(M, "RT_SynMod2D_Inv.rec"),
+                                                    33600 * 7).reshape(33600, 7)[:, :4])
+    assert np.array_equal(noisy[:, :2], fw_rec[:, :2])
+    P = os.path.join(REF, "par")
+    logs = {3: "RT_SynMod2D_Inv_RT.out", 1: "RT_SynMod2D_Inv_Trans.out", 2: "RT_SynMod2D_Inv_Ref.out"}
+    kw = {f"log_rttag{t}": np.array(trace_lines(os.path.join(P, f))) for t, f in logs.items()}
+    np.savez_compressed(os.path.join(HERE, "rt2d_inv_trace.npz"), tt=noisy[:, 4].copy(), tr=noisy[:, 5:7].copy(),
+                        nxy=noisy[:, 2:4].copy(), LM=50, nux=60.0, nuz=20.0, iters=TRACE_ITERS, **kw)
+
+
 def main():
+    if sys.argv[1:] == ["trace"]:
+        inversion_trace()
+        print("rt2d_inv_trace.npz written to", HERE)
+        return
     if not ref.available():
         build_ref.build()
     dx, dz = 12.5, 8.0
@@ -135,6 +173,7 @@ def main():
                         gRT_sha=sha(gRT), gT_sample=gT.ravel()[::997], gR_sample=gR.ravel()[::997])
     with open(os.path.join(HERE, "pins3d.json"), "w") as f:
         json.dump(pins3d(), f, indent=1)
+    inversion_trace()
     print("fixtures written to", HERE)
 
 

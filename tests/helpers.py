@@ -49,3 +49,10 @@ def picks_from(Ts, src, srnum, rec, noise, unpicked_offset=3):
         if len(rows) > unpicked_offset:
             tobs[rows[unpicked_offset]] = 1000.0
     return tobs
+
+
+def load_trace():
+    """Noisy picks of all 56 sources of the shipped inversion case and the reference's
+    printed iteration lines (tests/golden/rt2d_inv_trace.npz)."""
+    z = np.load(os.path.join(GOLDEN, "rt2d_inv_trace.npz"))
+    return {k: z[k] for k in z.files}
