@@ -46,6 +46,10 @@ typedef struct {
     int precision;   /* PFAST_PLAIN_FP64 or PFAST_MIXED */
     int maxswp;      /* MAXSwp: outer-iteration cap per solve (3D driver 100, 2D driver 500) */
     int max_batch;   /* sources per device batch; 0 = as many as fit */
+    double polish_floor;  /* mixed mode (3D): FP64 polish corrections of at most this many seconds
+                             (adjoint: times 1 + |lambda|) are dropped, so converged regions reach
+                             a bitwise fixed point; 0 = the default, 1e-10.  Keep it well below the
+                             1e-9 convergence tolerance. */
 } pfast_options;
 
 typedef struct {

@@ -24,7 +24,7 @@ PFAST_MIXED = 1
 
 
 class Options(C.Structure):
-    _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int)]
+    _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int), ("polish_floor", C.c_double)]
 
 
 class Stats(C.Structure):

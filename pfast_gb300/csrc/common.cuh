@@ -13,6 +13,10 @@ namespace pfast {
 constexpr double kInf = 9999999.0;
 // isconv tolerance (src/T_pfsm3d.h:126, src/RT_pfsm2d.h:112).
 constexpr double kConvTol = 1e-9;
+// Default polish floor: FP64 polish corrections at or below this (seconds, or relative to
+// 1 + |lambda| for the adjoint) are dropped, so converged regions reach a bitwise fixed
+// point; an order of magnitude under the 1e-9 convergence tolerance.
+constexpr float kPolishFloor = 1e-10f;
 
 // ---------------------------------------------------------------- 3D tiles
 // One warp sweeps one TK x TI x TJ tile.  Lane = (lk, li), TK*TI == 32; each lane

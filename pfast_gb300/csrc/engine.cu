@@ -164,7 +164,11 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     a.diff = a.stamp + ntiles * nb;
     cudaStream_t st = ctx->stream;
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
-    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0x01, sizeof(int) * ntiles * nb, st));
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0xff, sizeof(int) * ntiles * nb, st));
+    PFAST_TRY(ctx->work.ensure(sizeof(unsigned long long) * nb));
+    PFAST_TRY(ctx->h_work.ensure(sizeof(unsigned long long) * nb));
+    a.work = ctx->work.as<unsigned long long>();
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.work, 0, sizeof(unsigned long long) * nb, st));
     PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * nb, st));
     int it = 0;
     while (!active.empty() && it < maxiter) {
@@ -186,7 +190,6 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
         PFAST_CUDA_TRY(cudaStreamSynchronize(st));
         ++it;
-        if (node_updates) *node_updates += (long long)nact * 8 * nodes_per_sweep;
         std::vector<int> still;
         still.reserve(nact);
         for (int id : active) {
@@ -197,6 +200,12 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     }
     if (not_conv) *not_conv += (int)active.size();
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[1], st));
+    if (node_updates) {
+        unsigned long long* hw = ctx->h_work.as<unsigned long long>();
+        PFAST_CUDA_TRY(cudaMemcpyAsync(hw, a.work, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, st));
+        PFAST_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int b = 0; b < nb; ++b) *node_updates += (long long)hw[b];
+    }
     add_elapsed(ctx->ev[0], ctx->ev[1], ms_acc);
     return PFAST_OK;
 }
@@ -209,6 +218,7 @@ Sweep3Args base_args(const pfast_survey3d* sv) {
     a.nc = sv->nc;
     a.sp = make_spacing(sv->dx, sv->dy, sv->dz);
     a.wpr = (sv->nc + 31) / 32;
+    a.polish_floor = kPolishFloor;
     return a;
 }
 
@@ -286,6 +296,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.snap = ctx->scratch.p;
         a.aux = ctx->sq64.p;
         a.slow64 = ctx->s64.as<double>();
+        a.polish_floor = ctx->polish_floor;
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
@@ -392,6 +403,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.field = ctx->L64.p;
         a.snap = ctx->scratch.p;
         a.aux = ctx->T64.p;
+        a.polish_floor = ctx->polish_floor;
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
@@ -417,6 +429,10 @@ bool valid_options(const pfast_options* opt) {
         set_last_error("negative maxswp / max_batch");
         return false;
     }
+    if (!(opt->polish_floor >= 0.0 && opt->polish_floor < 1e-9)) {
+        set_last_error("polish_floor must be in [0, 1e-9)");
+        return false;
+    }
     return true;
 }
 
@@ -425,6 +441,7 @@ pfast_options resolve(const pfast_options* opt, int default_maxswp) {
     o.precision = PFAST_PLAIN_FP64;
     o.maxswp = default_maxswp;
     o.max_batch = 0;
+    o.polish_floor = 0.0;
     if (opt) o = *opt;
     return o;
 }
@@ -478,6 +495,7 @@ void pfast_default_options(pfast_options* opt) {
     opt->precision = PFAST_PLAIN_FP64;
     opt->maxswp = 100;
     opt->max_batch = 0;
+    opt->polish_floor = 0.0;
 }
 
 pfast_status pfast_ctx_create(int device, pfast_ctx** out) {
@@ -510,9 +528,9 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->sq64, &ctx->T32, &ctx->tflags, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
                       &ctx->ee, &ctx->need, &ctx->misc, &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a,
-                      &ctx->f2b, &ctx->f2c})
+                      &ctx->f2b, &ctx->f2c, &ctx->work})
         b->release();
-    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need}) b->release();
+    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work}) b->release();
     for (auto& kv : ctx->diag3) free_diag_table3(kv.second);
     for (auto& kv : ctx->diag2) free_diag_table2(kv.second);
     for (auto& ev : ctx->ev)
@@ -632,6 +650,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     const bool want_grad = grad != nullptr;
     if (want_grad && !sv->has_picks) { set_last_error("survey has no picks: gradient unavailable"); return PFAST_ERR_INVALID; }
     pfast_options o = resolve(opt, 100);
+    ctx->polish_floor = o.polish_floor > 0.0 ? (float)o.polish_floor : kPolishFloor;
     stats_begin(stats);
     PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
     const long long N = (long long)sv->nz * sv->nr * sv->nc;

@@ -43,11 +43,13 @@ struct pfast_ctx {
     // device work buffers (reused across calls)
     pfast::DevBuf s64, s32, sq64, T32, tflags, T64, L64, scratch, mask, act, changed, ee, need, misc, grad_tmp, vp_tmp, picks_tmp;
     pfast::DevBuf f2a, f2b, f2c;       // 2D field buffers
-    pfast::HostBuf h_act, h_changed, h_ee, h_need;
+    pfast::HostBuf h_act, h_changed, h_ee, h_need, h_work;
+    pfast::DevBuf work;                 // executed node updates per instance (sweep kernels)
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
     std::map<std::pair<int, int>, pfast::DiagTable2> diag2;
     cudaEvent_t ev[8] = {};
     long long launches = 0;
+    float polish_floor = pfast::kPolishFloor;   // of the current 3D evaluation (pfast_options)
 };
 
 struct pfast_survey3d {

@@ -31,11 +31,14 @@ struct Sweep3Args {
     int dir;                  // sweep order 0..7: bit2 = s3>0 (z), bit1 = s1>0 (rows), bit0 = s2>0 (cols)
     int iter;                 // outer-iteration index (snapshot stamps)
     int ntiles;               // tiles per instance (nbk*nbi*nbj)
-    int* dirty;               // per (instance, tile): process the tile (see sweep3d_kernel)
+    int* dirty;               // per (instance, tile): sweep orders still to process (see sweep3d_kernel)
     int* stamp;               // per (instance, tile): iteration of the tile's snapshot
     int* diff;                // per (instance, tile): differs from its snapshot by > tol
     double tol_abs, tol_rel;  // change test: |new-old| > tol_abs + tol_rel*|new| (FP64 sweeps)
     float tol_abs_f, tol_rel_f;  // the same test for the FP32 sweeps, evaluated in FP32
+    float polish_floor;       // polish sweeps: corrections at or below this are dropped (seconds;
+                              // adjoint: relative to 1 + |lambda|)
+    unsigned long long* work; // per instance: nodes of the tiles processed (executed node updates); may be null
 };
 
 // Tile-diagonal table for a grid: tiles (bk, bi, bj) in flipped coordinates with

@@ -46,9 +46,6 @@ __host__ __device__ constexpr int warp_smem_bytes() {
 
 __device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
 
-// Polish corrections below this (seconds, or relative for the adjoint) are dropped;
-// two orders of magnitude under the 1e-9 convergence tolerance.
-constexpr float kPolishFloor = 1e-11f;
 
 // ----------------------------------------------------------- node updates
 // Reference Godunov update (src/T_pfsm3d.h:99-119).  a/b/c: neighbour minima along
@@ -113,7 +110,7 @@ __device__ __forceinline__ float eik3_fast(float a, float b, float c, float s, c
 // s2 = s^2 (precomputed); the rare restart branch (U0 at or below every
 // neighbour) takes the 1-term value with the slowness itself.
 __device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s2, const double* slow,
-                                              long long node, const Spacing3& sp) {
+                                              long long node, const Spacing3& sp, float floor) {
     const double px = pos_sign(U0 - a), py = pos_sign(U0 - b), pz = pos_sign(U0 - c);
     double f, g;
     if (sp.iso) {
@@ -133,7 +130,7 @@ __device__ __forceinline__ double eik3_newton(double U0, double a, double b, dou
     const float step = __fdividef((float)f, fp);
     // corrections far below the 1e-9 convergence tolerance are dropped, so that a
     // converged region reaches a bitwise fixed point (and its tiles lock)
-    return fabsf(step) <= kPolishFloor ? U0 : U0 - (double)step;
+    return fabsf(step) <= floor ? U0 : U0 - (double)step;
 }
 
 // Adjoint updates.  The reference's upwind formula (src/T_padjoint3d.h:51-66)
@@ -194,7 +191,7 @@ __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float
 // r = num - den*lambda0 in FP64 (max(+-e, 0) by the sign bit), the step r/den in FP32.
 __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm, double Typ, double Tym, double Tzp,
                                               double Tzm, double Lxp, double Lxm, double Lyp, double Lym, double Lzp,
-                                              double Lzm, double L0, const Spacing3& sp) {
+                                              double Lzm, double L0, const Spacing3& sp, float floor) {
     if (unreached64(T0, Txp, Txm, Typ, Tym, Tzp, Tzm)) return 0.0;
     const double exp_ = Txp - T0, exm = Txm - T0, eyp = Typ - T0, eym = Tym - T0, ezp = Tzp - T0, ezm = Tzm - T0;
     double num, den;   // den is accumulated with the sign flipped: -sum w min(e, 0)
@@ -214,7 +211,7 @@ __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm,
     if (!(dbits(den) > dbits(1e-9))) return 0.0;   // den >= 0 by construction
     const double r = fma(-den, L0, num);
     const float step = __fdividef((float)r, (float)den);
-    return fabsf(step) <= kPolishFloor * (1.0f + fabsf((float)L0)) ? L0 : L0 + (double)step;
+    return fabsf(step) <= floor * (1.0f + fabsf((float)L0)) ? L0 : L0 + (double)step;
 }
 
 // ----------------------------------------------------------- tile I/O
@@ -254,12 +251,46 @@ __device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0
     }
 }
 
+// ----------------------------------------------------------- octant selection (polish)
+// Sweep order o: bit 0 = columns ascending, bit 1 = rows ascending, bit 2 = z ascending.
+// Order masks: bit o set for the orders with that axis ascending / descending.
+constexpr unsigned kAscX = 0xaa, kDescX = 0x55, kAscY = 0xcc, kDescY = 0x33, kAscZ = 0xf0, kDescZ = 0x0f;
+
+// Forward polish: the orders in which every active axis (U0 above its smaller neighbour)
+// visits that smaller neighbour before the node, so the Newton step reads refreshed upwind
+// values.  Arguments are bit patterns of values >= 0 (lo = index - 1, hi = index + 1).
+__device__ __forceinline__ unsigned fwd_orders(long long u, long long xlo, long long xhi, long long ylo,
+                                               long long yhi, long long zlo, long long zhi) {
+    unsigned m = 0xff;
+    if (u > (xlo < xhi ? xlo : xhi)) m &= xlo < xhi ? kAscX : (xhi < xlo ? kDescX : 0xffu);
+    if (u > (ylo < yhi ? ylo : yhi)) m &= ylo < yhi ? kAscY : (yhi < ylo ? kDescY : 0xffu);
+    if (u > (zlo < zhi ? zlo : zhi)) m &= zlo < zhi ? kAscZ : (zhi < zlo ? kDescZ : 0xffu);
+    return m;
+}
+
+// Adjoint polish: lambda at a node depends on the neighbours with a larger traveltime.
+// Where exactly one neighbour of an axis is larger, the orders that visit it first;
+// where both are (or neither), any order.
+__device__ __forceinline__ unsigned adj_orders(long long t, long long xlo, long long xhi, long long ylo,
+                                               long long yhi, long long zlo, long long zhi) {
+    unsigned m = 0xff;
+    const bool a = xlo > t, b = xhi > t, c = ylo > t, d = yhi > t, e = zlo > t, f = zhi > t;
+    if (a != b) m &= a ? kAscX : kDescX;
+    if (c != d) m &= c ? kAscY : kDescY;
+    if (e != f) m &= e ? kAscZ : kDescZ;
+    return m;
+}
+
 // ----------------------------------------------------------- the sweep kernel
-// Tile locking: a tile whose last processing changed no bit of its field, and none
-// of whose face neighbours has changed a face node since, is a fixed point of the
-// node update in every sweep order (each node's update returned its own value
-// with the neighbour values it still has), so it is skipped.  Per (source, tile):
-//   dirty[t]  set by the tile itself or a face neighbour when a node changes,
+// Tile locking: a tile whose processing changed no bit of its field, and none of
+// whose face neighbours has changed a face node since, is a fixed point of the node
+// update for that sweep order (each node's update returned its own value with the
+// neighbour values it still has).  For the plain and FP32 updates the node update does
+// not depend on the order, so one quiet processing locks the tile for all eight; the
+// polish updates select nodes by sweep order (octant selection), so a tile locks for
+// an order only once it has been quiet in that order.  Per (source, tile):
+//   dirty[t]  bit o set: process the tile in sweep order o; all eight bits are set by
+//             the tile itself or a face neighbour when a node changes,
 //   stamp[t]  outer iteration in which the tile last took its snapshot,
 //   diff[t]   whether the tile differs from its snapshot by more than the
 //             tolerance after its latest processing (cleared each iteration).
@@ -288,9 +319,19 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const int tj = px ? bjf : A.nbj - 1 - bjf;
     const int tid = (tk * A.nbi + ti) * A.nbj + tj;
     int* dirty = A.dirty + (long long)inst * A.ntiles;
-    if (!dirty[tid]) return;   // locked tile (warp-uniform)
+    const int dmask = dirty[tid];
+    const int obit = 1 << A.dir;
+    constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
+    // polish kinds: bits 8-15 hold the orders in which some node of the tile is selected
+    // (recorded at the tile's last processing; all eight before the first)
+    const int omask = kSelective ? (dmask >> 8) & 0xff : 0xff;
+    if (!(dmask & omask & obit)) return;   // locked tile for this order (warp-uniform)
     __syncwarp();
-    if (lane == 0) dirty[tid] = 0;   // face neighbours run in other launches: no race
+    if (lane == 0) {
+        dirty[tid] = kSelective ? (dmask & ~obit) : 0;   // face neighbours run in other launches: no race
+        if (A.work) atomicAdd(A.work + inst, (unsigned long long)(min(TK, A.nz - tk * TK) * min(TI, A.nr - ti * TI) *
+                                                                  min(TJ, A.nc - tj * TJ)));
+    }
 
     const int k0 = tk * TK, i0 = ti * TI, j0 = tj * TJ;
     const int ek = min(TK, A.nz - k0), ei = min(TI, A.nr - i0), ej = min(TJ, A.nc - j0);
@@ -342,6 +383,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     int sk = -1, si = -1, sj = -1;
     if constexpr (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
     const bool row_interior = ADJ ? (gk >= 1 && gk <= nz - 2 && gi >= 1 && gi <= nr - 2) : true;
+    unsigned sel = 0;   // polish: orders in which some node of this lane's pencil is selected
     const long long rowbase = gk * plane + (long long)gi * nc;
     bool chg = false, chg_jlo = false, chg_jhi = false;   // this lane's pencil changed (anywhere / at lj = 0 / at ej-1)
 
@@ -368,10 +410,22 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                         const float zc = ref_min(box[c - PS], box[c + PS]);
                         nv = ref_min(old, eik3_fast(xa, yb, zc, s, A.sp));
                     } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2)
-                        const double xa = min_nonneg(box[c + 1], box[c - 1]);
-                        const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
-                        const double zc = min_nonneg(box[c - PS], box[c + PS]);
-                        nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp);
+                        // Octant selection: if an axis is active (U0 above its smaller neighbour) and
+                        // that neighbour is the one this sweep visits after the node, the update would
+                        // read a value the sweep has not refreshed; the node keeps its value and is
+                        // updated by the sweep that visits its upwind neighbours first.  A Newton step
+                        // is not monotone, so without this every sweep would move every node.
+                        // Integer compares of the bit patterns (values >= 0).
+                        const unsigned m = fwd_orders(dbits(old), dbits(box[c - 1]), dbits(box[c + 1]),
+                                                      dbits(box[c - HJ]), dbits(box[c + HJ]), dbits(box[c - PS]),
+                                                      dbits(box[c + PS]));
+                        sel |= m;
+                        if (m & obit) {
+                            const double xa = min_nonneg(box[c + 1], box[c - 1]);
+                            const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
+                            const double zc = min_nonneg(box[c - PS], box[c + PS]);
+                            nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp, A.polish_floor);
+                        }
                     }
                 }
             } else {
@@ -385,9 +439,18 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                                        aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
                                        box[c - PS], old, A.sp);
                     } else {
-                        nv = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                         aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                         box[c - PS], old, A.sp);
+                        // Octant selection (see the forward polish): lambda at a node depends on the
+                        // neighbours with a larger traveltime.  Where on some axis only the neighbour
+                        // visited after the node is larger, the node waits for its own sweep; where
+                        // both are larger no sweep order has both fresh, and the node is updated.
+                        const unsigned m = adj_orders(dbits(aux[c]), dbits(aux[c - 1]), dbits(aux[c + 1]),
+                                                      dbits(aux[c - HJ]), dbits(aux[c + HJ]), dbits(aux[c - PS]),
+                                                      dbits(aux[c + PS]));
+                        sel |= m;
+                        if (m & obit)
+                            nv = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
+                                             aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ],
+                                             box[c + PS], box[c - PS], old, A.sp, A.polish_floor);
                     }
                 }
             }
@@ -404,6 +467,11 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
         __syncwarp();
     }
 
+    if constexpr (kSelective) {
+        const unsigned tsel = __reduce_or_sync(0xffffffffu, sel);
+        if (lane == 0) dirty[tid] = (dirty[tid] & 0xff) | (int)(tsel << 8);
+    }
+
     // ---- nothing changed: the field and its snapshot comparison stand as they are
     if (!__any_sync(0xffffffffu, chg)) return;
 
@@ -415,14 +483,16 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
     const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
     if (lane == 0) {
+        // neighbours keep their selection bits: OR in the eight order bits (two tiles of one
+        // launch can share a face neighbour, hence atomic)
         const int sk_ = A.nbi * A.nbj;
-        dirty[tid] = 1;
-        if (f_klo && tk > 0) dirty[tid - sk_] = 1;
-        if (f_khi && tk < A.nbk - 1) dirty[tid + sk_] = 1;
-        if (f_ilo && ti > 0) dirty[tid - A.nbj] = 1;
-        if (f_ihi && ti < A.nbi - 1) dirty[tid + A.nbj] = 1;
-        if (f_jlo && tj > 0) dirty[tid - 1] = 1;
-        if (f_jhi && tj < A.nbj - 1) dirty[tid + 1] = 1;
+        dirty[tid] |= 0xff;
+        if (f_klo && tk > 0) atomicOr(dirty + tid - sk_, 0xff);
+        if (f_khi && tk < A.nbk - 1) atomicOr(dirty + tid + sk_, 0xff);
+        if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xff);
+        if (f_ihi && ti < A.nbi - 1) atomicOr(dirty + tid + A.nbj, 0xff);
+        if (f_jlo && tj > 0) atomicOr(dirty + tid - 1, 0xff);
+        if (f_jhi && tj < A.nbj - 1) atomicOr(dirty + tid + 1, 0xff);
     }
 
     // ---- write back and compare with the iteration-start snapshot

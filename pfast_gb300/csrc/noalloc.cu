@@ -184,7 +184,7 @@ extern "C" pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src
     a.dirty = d_dirty;
     a.stamp = d_dirty + ntiles;
     a.diff = d_dirty + 2 * ntiles;
-    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0x01, sizeof(int) * ntiles, s));
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0xff, sizeof(int) * ntiles, s));
     PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles, s));
     // outer iterations of src/T_pfsm3d.h:152: snapshot + 8 sweeps while some node moved by > 1e-9
     for (int it = 0; it < MAXSwp; ++it) {
