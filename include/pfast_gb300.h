@@ -50,7 +50,13 @@ typedef struct {
                              (adjoint: times 1 + |lambda|) are dropped, so converged regions reach
                              a bitwise fixed point; 0 = the default, 1e-10.  Keep it well below the
                              1e-9 convergence tolerance. */
+    int schedule;         /* 3D sweeps: 0 = automatic, 1 = one launch per tile diagonal (every tile of
+                             every source spread over all SMs), 2 = persistent (one block solves one
+                             source; automatic picks it from 4 sources per SM).  Same results. */
 } pfast_options;
+#define PFAST_SCHEDULE_AUTO 0
+#define PFAST_SCHEDULE_DIAGONAL 1
+#define PFAST_SCHEDULE_PERSISTENT 2
 
 typedef struct {
     long long fwd_node_updates;   /* executed node updates, forward sweeps (all precisions) */

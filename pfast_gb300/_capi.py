@@ -21,10 +21,12 @@ PFAST_ERR_LINE_SEARCH = 8
 
 PFAST_PLAIN_FP64 = 0
 PFAST_MIXED = 1
+PFAST_SCHEDULE_AUTO, PFAST_SCHEDULE_DIAGONAL, PFAST_SCHEDULE_PERSISTENT = 0, 1, 2
 
 
 class Options(C.Structure):
-    _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int), ("polish_floor", C.c_double)]
+    _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int), ("polish_floor", C.c_double),
+                ("schedule", C.c_int)]
 
 
 class Stats(C.Structure):

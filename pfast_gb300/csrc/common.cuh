@@ -33,6 +33,8 @@ static_assert(PS >= HI * HJ && (PS - 1) % 32 == 8 && (HJ - 1) % 32 == 1, "bank-c
 constexpr int SJ = TJ + 2, SPS = 297;
 static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
 // Warps (tiles) per CTA.
+constexpr int kMaxPWarps = 16;   // warps per block of the persistent sweep kernel, at most
+constexpr int kPersistentPerSM = 4;   // instances per SM from which the persistent schedule is used
 constexpr int kWarps3 = 1;   // one-warp CTAs: the finest shared-memory granularity, hence the most warps per SM
 
 // ---------------------------------------------------------------- 2D tiles
@@ -78,6 +80,13 @@ enum SweepKind : int {
 };
 
 }  // namespace pfast
+
+// Return a failing pfast_status from the enclosing function.
+#define PFAST_TRY(expr)                          \
+    do {                                         \
+        pfast_status s__ = (expr);               \
+        if (s__ != PFAST_OK) return s__;         \
+    } while (0)
 
 #define PFAST_CUDA_TRY(expr)                                                        \
     do {                                                                            \

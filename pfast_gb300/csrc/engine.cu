@@ -34,11 +34,6 @@ pfast_status cuda_fail(cudaError_t e, const char* what, const char* file, int li
     return e == cudaErrorMemoryAllocation ? PFAST_ERR_NOMEM : PFAST_ERR_CUDA;
 }
 
-#define PFAST_TRY(expr)                          \
-    do {                                         \
-        pfast_status s__ = (expr);               \
-        if (s__ != PFAST_OK) return s__;         \
-    } while (0)
 
 // ------------------------------------------------------------------ buffers
 pfast_status DevBuf::ensure(size_t bytes) {
@@ -170,8 +165,37 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     a.work = ctx->work.as<unsigned long long>();
     PFAST_CUDA_TRY(cudaMemsetAsync(a.work, 0, sizeof(unsigned long long) * nb, st));
     PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * nb, st));
+    // Two schedules.  Per-diagonal launches spread every tile of every active instance over
+    // all SMs (one warp per tile) and suit surveys with few instances per SM, such as 256
+    // sources on 152 SMs; the persistent kernel (one block solves one instance, no host
+    // round trip per iteration) suits runs with several instances per SM.
+    int dev = 0, sms = 1;
+    PFAST_CUDA_TRY(cudaGetDevice(&dev));
+    PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const bool persistent = ctx->schedule == PFAST_SCHEDULE_PERSISTENT ||
+                            (ctx->schedule == PFAST_SCHEDULE_AUTO && (int)active.size() >= kPersistentPerSM * sms);
+    if (persistent && maxiter > 0) {
+        const int nact = (int)active.size();
+        std::memcpy(h_act, active.data(), sizeof(int) * nact);
+        PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
+        PFAST_TRY(ctx->queue.ensure(sizeof(int)));
+        PFAST_CUDA_TRY(cudaMemsetAsync(ctx->queue.p, 0, sizeof(int), st));
+        a.ndiag = dt.ndiag;
+        int warps = 1, blocks = 1;
+        PFAST_TRY(persistent_shape(kind, nact, &warps, &blocks));
+        PFAST_TRY(launch_sweep3_persistent(kind, a, nact, maxiter, ctx->queue.as<int>(), a.changed, warps, blocks, st));
+        ++ctx->launches;
+        PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+        PFAST_CUDA_TRY(cudaStreamSynchronize(st));
+        std::vector<int> still;
+        for (int id : active) {
+            iters[id] = h_chg[id] & 0xffff;
+            if (h_chg[id] >> 30) still.push_back(id);
+        }
+        active.swap(still);
+    }
     int it = 0;
-    while (!active.empty() && it < maxiter) {
+    while (!persistent && !active.empty() && it < maxiter) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
@@ -433,6 +457,10 @@ bool valid_options(const pfast_options* opt) {
         set_last_error("polish_floor must be in [0, 1e-9)");
         return false;
     }
+    if (opt->schedule < PFAST_SCHEDULE_AUTO || opt->schedule > PFAST_SCHEDULE_PERSISTENT) {
+        set_last_error("unknown schedule %d", opt->schedule);
+        return false;
+    }
     return true;
 }
 
@@ -442,6 +470,7 @@ pfast_options resolve(const pfast_options* opt, int default_maxswp) {
     o.maxswp = default_maxswp;
     o.max_batch = 0;
     o.polish_floor = 0.0;
+    o.schedule = PFAST_SCHEDULE_AUTO;
     if (opt) o = *opt;
     return o;
 }
@@ -496,6 +525,7 @@ void pfast_default_options(pfast_options* opt) {
     opt->maxswp = 100;
     opt->max_batch = 0;
     opt->polish_floor = 0.0;
+    opt->schedule = PFAST_SCHEDULE_AUTO;
 }
 
 pfast_status pfast_ctx_create(int device, pfast_ctx** out) {
@@ -528,7 +558,7 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->sq64, &ctx->T32, &ctx->tflags, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
                       &ctx->ee, &ctx->need, &ctx->misc, &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a,
-                      &ctx->f2b, &ctx->f2c, &ctx->work})
+                      &ctx->f2b, &ctx->f2c, &ctx->work, &ctx->queue})
         b->release();
     for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work}) b->release();
     for (auto& kv : ctx->diag3) free_diag_table3(kv.second);
@@ -651,6 +681,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     if (want_grad && !sv->has_picks) { set_last_error("survey has no picks: gradient unavailable"); return PFAST_ERR_INVALID; }
     pfast_options o = resolve(opt, 100);
     ctx->polish_floor = o.polish_floor > 0.0 ? (float)o.polish_floor : kPolishFloor;
+    ctx->schedule = o.schedule;
     stats_begin(stats);
     PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
@@ -785,6 +816,7 @@ pfast_status pfast_fsm3d(double* vp, double* U, int* src, int srcid, int MAXSwp,
         if (e != cudaSuccess) r = cuda_fail(e, "copy vp", __FILE__, __LINE__);
     }
     if (!r) r = prepare_slowness(ctx, ctx->vp_tmp.as<double>(), N, false);
+    ctx->schedule = PFAST_SCHEDULE_AUTO;
     if (!r) r = forward3d_batch(ctx, sv, 0, 1, PFAST_PLAIN_FP64, MAXSwp, nullptr);
     if (!r) {
         cudaError_t e = cudaMemcpyAsync(U, ctx->T64.p, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
@@ -818,6 +850,7 @@ pfast_status pfast_adjoint_fsm3d(double* U, double* T, double* T_obs, int* rec, 
         if (e != cudaSuccess) r = cuda_fail(e, "copy T", __FILE__, __LINE__);
     }
     double ee = 0.0;
+    ctx->schedule = PFAST_SCHEDULE_AUTO;
     if (!r) r = adjoint3d_batch(ctx, sv, 0, 1, PFAST_PLAIN_FP64, MAXSwp, &ee, nullptr);
     if (!r) {
         cudaError_t e = cudaMemcpyAsync(U, ctx->L64.p, sizeof(double) * N, cudaMemcpyDeviceToHost, s);

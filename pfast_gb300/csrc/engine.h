@@ -45,11 +45,13 @@ struct pfast_ctx {
     pfast::DevBuf f2a, f2b, f2c;       // 2D field buffers
     pfast::HostBuf h_act, h_changed, h_ee, h_need, h_work;
     pfast::DevBuf work;                 // executed node updates per instance (sweep kernels)
+    pfast::DevBuf queue;                // work counter of the persistent sweep kernel
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
     std::map<std::pair<int, int>, pfast::DiagTable2> diag2;
     cudaEvent_t ev[8] = {};
     long long launches = 0;
     float polish_floor = pfast::kPolishFloor;   // of the current 3D evaluation (pfast_options)
+    int schedule = PFAST_SCHEDULE_AUTO;         // of the current 3D evaluation (pfast_options)
 };
 
 struct pfast_survey3d {

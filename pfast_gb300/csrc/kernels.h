@@ -27,6 +27,7 @@ struct Sweep3Args {
     const unsigned* diag_tiles;  //   diag_tiles[diag_off[d] .. diag_off[d+1])
     int nz, nr, nc;
     int nbk, nbi, nbj;
+    int ndiag;                // tile diagonals (persistent kernel)
     Spacing3 sp;
     int dir;                  // sweep order 0..7: bit2 = s3>0 (z), bit1 = s1>0 (rows), bit0 = s2>0 (cols)
     int iter;                 // outer-iteration index (snapshot stamps)
@@ -57,6 +58,14 @@ size_t sweep3_smem_bytes(int kind);
 // changed[act[b]] = any diff over the tiles of instance act[b], b < nact.
 pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
+// Persistent sweep kernel: `blocks` blocks of `warps` warps take the nact instances of a.act
+// from *queue (zeroed by the caller) and solve each to convergence (maxiter outer
+// iterations at most); result[inst] = iterations | 1<<30 if not converged.
+pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
+                                      int warps, int blocks, cudaStream_t st);
+// Warps per block and resident blocks for the persistent kernel: the most warps per block
+// that still let every SM hold ceil(nact / SMs) blocks.
+pfast_status persistent_shape(int kind, int nact, int* warps, int* blocks);
 
 // Small 3D kernels.
 // s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64 (if non-null); *bad is set

@@ -17,6 +17,8 @@
 // step in FP32, so the fixed point is the FP64 one while FP64 issue slots (about 2
 // lanes per clock per SM on this part) go only where the precision is needed.
 
+#include <map>
+#include <mutex>
 #include <vector>
 #include <algorithm>
 #include <type_traits>
@@ -219,7 +221,9 @@ __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm,
 // (plane stride PS, row stride HJ), one box row per warp instruction (lanes along
 // the row, coalesced); out-of-grid entries get `fill`.  Twelve rows are loaded
 // before they are stored, to keep many loads in flight.
-template <typename T>
+// COHERENT: the field, which the persistent kernel itself writes (other warps of the block
+// stored the neighbouring tiles): read through L2, not the read-only path.
+template <typename T, bool COHERENT>
 __device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0, int i0, int j0, int nz, int nr,
                                          int nc, T fill, int lane) {
     constexpr int NROW = HK * HI;
@@ -238,8 +242,13 @@ __device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0
             const int gk = k0 - 1 + z, gi = i0 - 1 + y;
             const bool rok = (unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr;
             const T* row = g + gk * plane + (long long)gi * nc;
-            v0[u] = (rok && c0) ? __ldg(row + gj0) : fill;
-            v1[u] = (rok && c1) ? __ldg(row + gj1) : fill;
+            if constexpr (COHERENT) {
+                v0[u] = (rok && c0) ? __ldcg(row + gj0) : fill;
+                v1[u] = (rok && c1) ? __ldcg(row + gj1) : fill;
+            } else {
+                v0[u] = (rok && c0) ? __ldg(row + gj0) : fill;
+                v1[u] = (rok && c1) ? __ldg(row + gj1) : fill;
+            }
         }
 #pragma unroll
         for (int u = 0; u < RB; ++u) {
@@ -296,38 +305,44 @@ __device__ __forceinline__ unsigned adj_orders(long long t, long long xlo, long 
 //             tolerance after its latest processing (cleared each iteration).
 // The outer-iteration test of the reference (isconv) is the OR of diff over the
 // tiles of a source: a skipped tile has not moved.
+// Tile (tk, ti, tj) and its index of the diagonal-table entry pk in sweep order dir (the
+// table is in flipped coordinates).
+__device__ __forceinline__ int tile_of(const Sweep3Args& A, unsigned pk, int dir, int& tk, int& ti, int& tj) {
+    const int bkf = pk & 1023, bif = (pk >> 10) & 1023, bjf = pk >> 20;
+    tk = (dir & 4) ? bkf : A.nbk - 1 - bkf;
+    ti = (dir & 2) ? bif : A.nbi - 1 - bif;
+    tj = (dir & 1) ? bjf : A.nbj - 1 - bjf;
+    return (tk * A.nbi + ti) * A.nbj + tj;
+}
+
+// Whether a tile with lock word dm is processed in sweep order dir.  Polish kinds: bits 8-15
+// hold the orders in which some node of the tile is selected (recorded at the tile's last
+// processing; all eight before the first).
 template <int KIND>
-__global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args A, const int d) {
+__device__ __forceinline__ bool tile_due(int dm, int dir) {
+    constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
+    const int omask = kSelective ? (dm >> 8) & 0xff : 0xff;
+    return (dm & omask & (1 << dir)) != 0;
+}
+
+// One warp processes one tile (inst, tid) in sweep order dir, outer iteration iter; dmask is
+// the tile's lock word as read by the caller, which has checked tile_due.  wsm: the warp's
+// shared-memory slice.  COHERENT: the field may have been written by this same kernel launch
+// (persistent schedule), so it is read through L2 instead of the read-only path.
+template <int KIND, bool COHERENT>
+__device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst, const int tid, const int tk,
+                                             const int ti, const int tj, const int dir, const int iter,
+                                             const int dmask, unsigned char* wsm, const int lane) {
     using Real = typename Traits<KIND>::Real;
     using Aux = typename Traits<KIND>::Aux;
     using Bits = typename std::conditional<sizeof(Real) == 8, unsigned long long, unsigned>::type;
     constexpr bool ADJ = Traits<KIND>::adj;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int d0 = A.diag_off[d];
-    const int tile_idx = blockIdx.x * kWarps3 + warp;
-    if (tile_idx >= A.diag_off[d + 1] - d0) return;
-    const int inst = A.act[blockIdx.y];
-
-    // ---- tile placement (the diagonal table is in flipped coordinates)
-    const unsigned pk = A.diag_tiles[d0 + tile_idx];
-    const bool pz = A.dir & 4, py = A.dir & 2, px = A.dir & 1;
-    const int bkf = pk & 1023, bif = (pk >> 10) & 1023, bjf = pk >> 20;
-    const int tk = pz ? bkf : A.nbk - 1 - bkf;
-    const int ti = py ? bif : A.nbi - 1 - bif;
-    const int tj = px ? bjf : A.nbj - 1 - bjf;
-    const int tid = (tk * A.nbi + ti) * A.nbj + tj;
+    const bool pz = dir & 4, py = dir & 2, px = dir & 1;
     int* dirty = A.dirty + (long long)inst * A.ntiles;
-    const int dmask = dirty[tid];
-    const int obit = 1 << A.dir;
+    const int obit = 1 << dir;
     constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
-    // polish kinds: bits 8-15 hold the orders in which some node of the tile is selected
-    // (recorded at the tile's last processing; all eight before the first)
-    const int omask = kSelective ? (dmask >> 8) & 0xff : 0xff;
-    if (!(dmask & omask & obit)) return;   // locked tile for this order (warp-uniform)
-    __syncwarp();
     if (lane == 0) {
+
         dirty[tid] = kSelective ? (dmask & ~obit) : 0;   // face neighbours run in other launches: no race
         if (A.work) atomicAdd(A.work + inst, (unsigned long long)(min(TK, A.nz - tk * TK) * min(TI, A.nr - ti * TI) *
                                                                   min(TJ, A.nc - tj * TJ)));
@@ -338,7 +353,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const int nz = A.nz, nr = A.nr, nc = A.nc;
     const long long plane = (long long)nr * nc;
 
-    Real* box = reinterpret_cast<Real*>(smem_raw + warp * warp_smem_bytes<KIND>());
+    Real* box = reinterpret_cast<Real*>(wsm);
     Aux* aux = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
     Real* fld = reinterpret_cast<Real*>(A.field) + inst * A.fstride;
     Real* snp = reinterpret_cast<Real*>(A.snap) + inst * A.fstride;
@@ -346,7 +361,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     // ---- stage the field halo box (out-of-grid: +inf for the forward so that the
     // neighbour minimum reduces to the one-sided rule at faces; never read by the adjoint)
     const Real fill = ADJ ? Real(0) : Real(INFINITY);
-    load_box<Real>(box, fld, k0, i0, j0, nz, nr, nc, fill, lane);
+    load_box<Real, COHERENT>(box, fld, k0, i0, j0, nz, nr, nc, fill, lane);
 
     // ---- auxiliary data
     unsigned fixed_bits = 0;
@@ -356,7 +371,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const int li = py ? lif : ei - 1 - lif;
     if constexpr (ADJ) {
         const Aux* T = reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride;
-        load_box<Aux>(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane);
+        load_box<Aux, false>(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane);
         if (lane_ok)
             fixed_bits = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
     }
@@ -364,7 +379,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     // ---- snapshot at the tile's first processing in this outer iteration (its values are
     // still the iteration-start values then: only the tile itself writes them)
     int* stamp = A.stamp + (long long)inst * A.ntiles;
-    if (stamp[tid] != A.iter) {
+    if (__ldcg(stamp + tid) != iter) {
 #pragma unroll 4
         for (int m = 0; m < 32; ++m) {
             const int rk = m / TI, ri = m % TI;
@@ -372,7 +387,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                 snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
                     box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
         }
-        if (lane == 0) stamp[tid] = A.iter;
+        if (lane == 0) stamp[tid] = iter;
     }
     __syncwarp();
 
@@ -504,7 +519,7 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
         for (int u = 0; u < 8; ++u) {
             const int m = m0 + u, rk = m / TI, ri = m % TI;
             p[u] = Real(0);
-            if (rk < ek && ri < ei && lane < ej) p[u] = snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane];
+            if (rk < ek && ri < ei && lane < ej) p[u] = __ldcg(snp + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane);
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
@@ -522,6 +537,98 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     }
     const bool any_moved = __any_sync(0xffffffffu, moved);
     if (lane == 0) A.diff[(long long)inst * A.ntiles + tid] = any_moved ? 1 : 0;
+}
+
+// One launch per tile diagonal: block (x, y) = (tile of the diagonal, active instance).
+template <int KIND>
+__global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args A, const int d) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d0 = A.diag_off[d];
+    const int tile_idx = blockIdx.x * kWarps3 + warp;
+    if (tile_idx >= A.diag_off[d + 1] - d0) return;
+    const int inst = A.act[blockIdx.y];
+    int tk, ti, tj;
+    const int tid = tile_of(A, A.diag_tiles[d0 + tile_idx], A.dir, tk, ti, tj);
+    const int dm = __ldcg(A.dirty + (long long)inst * A.ntiles + tid);
+    if (!tile_due<KIND>(dm, A.dir)) return;   // locked tile for this order (warp-uniform)
+    __syncwarp();
+    process_tile<KIND, false>(A, inst, tid, tk, ti, tj, A.dir, A.iter, dm, smem_raw + warp * warp_smem_bytes<KIND>(),
+                              lane);
+}
+
+// Persistent form: one launch per phase.  Each block takes instances (sources) from a
+// queue and runs the whole solve of one instance -- outer iterations of eight ordered
+// sweeps until the instance's convergence test passes or maxiter iterations ran -- with
+// the tile diagonals of a sweep separated by block barriers (all tiles of an instance
+// are processed by the one block, so the diagonal order needs no other synchronisation).
+// Per diagonal, the block reads the lock words of up to blockDim tiles at once, lists
+// the tiles due in shared memory, and its warps process the list.
+// result[inst] = iterations run, | 1<<30 when maxiter stopped the solve unconverged.
+template <int KIND>
+__global__ void __launch_bounds__(kMaxPWarps * 32) sweep3d_persistent(const Sweep3Args A, const int nact,
+                                                                     const int maxiter, int* __restrict__ queue,
+                                                                     int* __restrict__ result) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item, s_cnt;
+    __shared__ int s_list[kMaxPWarps * 32];
+    __shared__ int s_dm[kMaxPWarps * 32];
+    const int nthr = blockDim.x, nw = nthr >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wsm = smem_raw + warp * warp_smem_bytes<KIND>();
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= nact) return;   // block-uniform
+        const int inst = A.act[item];
+        int* diff = A.diff + (long long)inst * A.ntiles;
+        const int* dirty = A.dirty + (long long)inst * A.ntiles;
+        int it = 0;
+        bool moved = true;
+        while (it < maxiter) {
+            for (int t = threadIdx.x; t < A.ntiles; t += nthr) diff[t] = 0;
+            __syncthreads();
+            for (int dir = 0; dir < 8; ++dir) {
+                for (int d = 0; d < A.ndiag; ++d) {
+                    const int d0 = A.diag_off[d], cnt = A.diag_off[d + 1] - d0;
+                    for (int c0 = 0; c0 < cnt; c0 += nthr) {
+                        if (threadIdx.x == 0) s_cnt = 0;
+                        __syncthreads();
+                        const int idx = c0 + threadIdx.x;
+                        if (idx < cnt) {
+                            int tk, ti, tj;
+                            const int tid = tile_of(A, A.diag_tiles[d0 + idx], dir, tk, ti, tj);
+                            const int dm = __ldcg(dirty + tid);
+                            if (tile_due<KIND>(dm, dir)) {
+                                const int slot = atomicAdd(&s_cnt, 1);
+                                s_list[slot] = idx;
+                                s_dm[slot] = dm;
+                            }
+                        }
+                        __syncthreads();
+                        const int n = s_cnt;
+                        for (int q = warp; q < n; q += nw) {
+                            int tk, ti, tj;
+                            const int tid = tile_of(A, A.diag_tiles[d0 + s_list[q]], dir, tk, ti, tj);
+                            process_tile<KIND, true>(A, inst, tid, tk, ti, tj, dir, it, s_dm[q], wsm, lane);
+                        }
+                        __syncthreads();
+                    }
+                }
+            }
+            int any = 0;
+            for (int t = threadIdx.x; t < A.ntiles; t += nthr) any |= __ldcg(diff + t);
+            any = __syncthreads_or(any);
+            ++it;
+            if (!any) {
+                moved = false;
+                break;
+            }
+        }
+        if (threadIdx.x == 0) result[inst] = it | (moved ? (1 << 30) : 0);
+    }
 }
 
 // changed[act[b]] = OR over the tiles of instance act[b] of diff.
@@ -595,6 +702,98 @@ static pfast_status launch_one(const Sweep3Args& a, int d, int tiles, int nact, 
     dim3 grid((tiles + kWarps3 - 1) / kWarps3, nact);
     sweep3d_kernel<KIND><<<grid, kWarps3 * 32, smem, st>>>(a, d);
     return PFAST_OK;
+}
+
+template <int KIND>
+static pfast_status persistent_attr(int warps) {
+    static int set_for = 0;
+    const int smem = warps * warp_smem_bytes<KIND>();
+    if (set_for < smem) {
+        PFAST_CUDA_TRY(cudaFuncSetAttribute(sweep3d_persistent<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        set_for = smem;
+    }
+    return PFAST_OK;
+}
+
+template <int KIND>
+static pfast_status persistent_shape_k(int nact, int* warps, int* blocks) {
+    static std::map<std::pair<int, int>, std::pair<int, int>> cache;   // (device, nact) -> (warps, blocks)
+    static std::mutex mu;
+    int dev = 0, sms = 0, smem_max = 0;
+    PFAST_CUDA_TRY(cudaGetDevice(&dev));
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find({dev, nact});
+        if (it != cache.end()) {
+            *warps = it->second.first;
+            *blocks = it->second.second;
+            return PFAST_OK;
+        }
+    }
+    PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PFAST_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int need = std::max(1, (nact + sms - 1) / sms);   // blocks each SM must hold at once
+    const int w_cap = std::max(1, std::min(kMaxPWarps, (smem_max - 8192) / warp_smem_bytes<KIND>()));
+    int best_w = 1, best_b = 1;
+    for (int w = w_cap; w >= 1; --w) {
+        PFAST_TRY(persistent_attr<KIND>(w));
+        int per_sm = 0;
+        PFAST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep3d_persistent<KIND>, w * 32,
+                                                                     (size_t)w * warp_smem_bytes<KIND>()));
+        if (per_sm >= need || w == 1) {
+            best_w = w;
+            best_b = std::max(1, per_sm);
+            break;
+        }
+    }
+    *warps = best_w;
+    *blocks = std::min(nact, best_b * sms);
+    std::lock_guard<std::mutex> g(mu);
+    cache[{dev, nact}] = {*warps, *blocks};
+    return PFAST_OK;
+}
+
+template <int KIND>
+static pfast_status launch_persistent_k(const Sweep3Args& a, int nact, int maxiter, int* queue, int* result, int warps,
+                                        int blocks, cudaStream_t st) {
+    PFAST_TRY(persistent_attr<KIND>(warps));
+    sweep3d_persistent<KIND><<<blocks, warps * 32, (size_t)warps * warp_smem_bytes<KIND>(), st>>>(a, nact, maxiter,
+                                                                                                  queue, result);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "persistent sweep launch", __FILE__, __LINE__);
+    return PFAST_OK;
+}
+
+pfast_status persistent_shape(int kind, int nact, int* warps, int* blocks) {
+    switch (kind) {
+        case kFwdPlain64: return persistent_shape_k<kFwdPlain64>(nact, warps, blocks);
+        case kFwdFast32: return persistent_shape_k<kFwdFast32>(nact, warps, blocks);
+        case kFwdPolish64: return persistent_shape_k<kFwdPolish64>(nact, warps, blocks);
+        case kAdjPlain64: return persistent_shape_k<kAdjPlain64>(nact, warps, blocks);
+        case kAdjFast32: return persistent_shape_k<kAdjFast32>(nact, warps, blocks);
+        case kAdjPolish64: return persistent_shape_k<kAdjPolish64>(nact, warps, blocks);
+    }
+    set_last_error("unknown sweep kind %d", kind);
+    return PFAST_ERR_INVALID;
+}
+
+pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
+                                      int warps, int blocks, cudaStream_t st) {
+    if (nact <= 0 || maxiter <= 0) return PFAST_OK;
+    if (warps < 1 || warps > kMaxPWarps || blocks < 1) {
+        set_last_error("persistent sweep: bad shape (%d warps, %d blocks)", warps, blocks);
+        return PFAST_ERR_INVALID;
+    }
+    switch (kind) {
+        case kFwdPlain64: return launch_persistent_k<kFwdPlain64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kFwdFast32: return launch_persistent_k<kFwdFast32>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kFwdPolish64: return launch_persistent_k<kFwdPolish64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kAdjPlain64: return launch_persistent_k<kAdjPlain64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kAdjFast32: return launch_persistent_k<kAdjFast32>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kAdjPolish64: return launch_persistent_k<kAdjPolish64>(a, nact, maxiter, queue, result, warps, blocks, st);
+    }
+    set_last_error("unknown sweep kind %d", kind);
+    return PFAST_ERR_INVALID;
 }
 
 pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st) {
