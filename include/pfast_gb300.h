@@ -260,6 +260,78 @@ pfast_status pfast_inversion_get(pfast_inversion* inv, int field, double* host);
 pfast_status pfast_inversion_field(pfast_inversion* inv, int field, const double** dev);
 pfast_status pfast_inversion_destroy(pfast_inversion* inv);
 
+/* ------------------------------------------------------------------ request server
+ * No counterpart in the reference (its drivers run one survey per MPI job).  Continuous
+ * batching on one GPU: traveltime (forward) and misfit-gradient requests of any grid size
+ * arrive at any time; models and surveys stay resident on the device under an ID; a
+ * request starts as soon as one of `slots` workers is free and its device memory fits the
+ * HBM budget (resident data plus running requests), and running requests overlap on the
+ * GPU, each on its own stream.  Admission is first come first served, except that a
+ * younger request may overtake a waiting one that does not fit yet (at most `max_bypass`
+ * times); a request's source batch is sized to its memory allowance.  Results do not
+ * depend on what else runs: every request is computed exactly as it would be alone.
+ */
+typedef struct pfast_server pfast_server;
+
+typedef struct {
+    int device;
+    int slots;                 /* requests running at once (workers), >= 1 */
+    double hbm_budget_bytes;   /* device memory for resident models/surveys and running requests */
+    int max_bypass;            /* overtakes of a waiting request before it blocks admission (8) */
+} pfast_server_config;
+
+#define PFAST_REQ_FORWARD 0    /* picks: 3D [nrec]; 2D [nrec*(NumofR+1)] (TT then each reflector) */
+#define PFAST_REQ_GRADIENT 1   /* misfit and gradient [N]: 3D grad; 2D gRT = gT(1-WR) + gR WR */
+
+typedef struct {
+    int kind;                  /* PFAST_REQ_* */
+    long long model_id;        /* registered with pfast_server_put_model */
+    long long survey_id;       /* registered with pfast_server_put_survey3d / _2d (same grid) */
+    pfast_options opt;         /* precision, maxswp, polish_floor, schedule; max_batch: the server's */
+    double* out;               /* HOST output, written when the request completes */
+    double* out_misfit;        /* gradient: HOST scalar, E (3D) or Et + Er (2D); may be NULL */
+} pfast_request;
+
+typedef struct {
+    pfast_status status;       /* the request's own status */
+    int batch;                 /* sources solved at once */
+    double queue_ms;           /* submit -> start */
+    double run_ms;             /* start -> done */
+    double total_ms;           /* submit -> done */
+} pfast_request_result;
+
+typedef struct {
+    long long submitted, completed, failed;
+    int running, waiting;
+    int resident_models, resident_surveys;
+    double used_bytes, peak_bytes, budget_bytes;
+} pfast_server_stats;
+
+pfast_status pfast_server_create(const pfast_server_config* cfg, pfast_server** out);
+/* Waits for every submitted request, then frees everything. */
+pfast_status pfast_server_destroy(pfast_server* srv);
+/* A velocity model (HOST array [nz*nrows*ncols], nz = 1 in 2D) kept on the device under
+ * model_id; 2D gradient requests also need WR [nrows*ncols] (else NULL).  dim: 2 or 3.
+ * Replacing an ID that requests still use fails (PFAST_ERR_INVALID). */
+pfast_status pfast_server_put_model(pfast_server* srv, long long model_id, int dim, int nrows, int ncols, int nz,
+                                    double dx, double dy, double dz, const double* vp, const double* WR);
+/* Surveys, arguments as pfast_survey3d_create / pfast_survey2d_create (HOST arrays, copied). */
+pfast_status pfast_server_put_survey3d(pfast_server* srv, long long survey_id, int nrows, int ncols, int nz, double dx,
+                                       double dy, double dz, int nsrc, const int* src, const int* srnum,
+                                       const int* rec, const double* nxyz, const double* T_obs);
+pfast_status pfast_server_put_survey2d(pfast_server* srv, long long survey_id, int nrows, int ncols, double dx,
+                                       double dz, int nsrc, const int* src, const int* srnum, int nrec,
+                                       const int* rec, const double* nxy, const double* TT_obs, int NumofR,
+                                       const double* TR_obs, const double* Z);
+/* Forget a model (what = 0) or survey (what = 1); freed once no request uses it.  Unused
+ * resident entries are also evicted, least recently used first, when new data needs room. */
+pfast_status pfast_server_drop(pfast_server* srv, int what, long long id);
+/* Queue a request; *ticket identifies it.  The output buffers must stay valid until wait. */
+pfast_status pfast_server_submit(pfast_server* srv, const pfast_request* req, long long* ticket);
+/* Block until the request is done; returns its status (message in pfast_last_error). */
+pfast_status pfast_server_wait(pfast_server* srv, long long ticket, pfast_request_result* res);
+pfast_status pfast_server_stats_get(pfast_server* srv, pfast_server_stats* st);
+
 /* ------------------------------------------------------- no-allocation entry point
  * No counterpart in the reference.  The traveltime field of one point source --
  * the computation of pfast_fsm3d (plain FP64, bit-identical to it) -- for callers

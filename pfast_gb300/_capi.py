@@ -79,6 +79,36 @@ class InvertReport(C.Structure):
         return d
 
 
+PFAST_REQ_FORWARD, PFAST_REQ_GRADIENT = 0, 1
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("hbm_budget_bytes", C.c_double), ("max_bypass", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("model_id", C.c_longlong), ("survey_id", C.c_longlong), ("opt", Options),
+                ("out", C.c_void_p), ("out_misfit", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("batch", C.c_int), ("queue_ms", C.c_double), ("run_ms", C.c_double),
+                ("total_ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("running", C.c_int), ("waiting", C.c_int), ("resident_models", C.c_int),
+                ("resident_surveys", C.c_int), ("used_bytes", C.c_double), ("peak_bytes", C.c_double),
+                ("budget_bytes", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # (name, restype, argtypes) of every entry point in include/pfast_gb300.h
 _p, _i, _d = C.c_void_p, C.c_int, C.c_double
 SIGNATURES = [
@@ -117,6 +147,15 @@ SIGNATURES = [
     ("pfast_inversion_get", _i, [_p, _i, _p]),
     ("pfast_inversion_field", _i, [_p, _i, _p]),
     ("pfast_inversion_destroy", _i, [_p]),
+    ("pfast_server_create", _i, [_p, _p]),
+    ("pfast_server_destroy", _i, [_p]),
+    ("pfast_server_put_model", _i, [_p, C.c_longlong, _i, _i, _i, _i, _d, _d, _d, _p, _p]),
+    ("pfast_server_put_survey3d", _i, [_p, C.c_longlong, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p]),
+    ("pfast_server_put_survey2d", _i, [_p, C.c_longlong, _i, _i, _d, _d, _i, _p, _p, _i, _p, _p, _p, _i, _p, _p]),
+    ("pfast_server_drop", _i, [_p, _i, C.c_longlong]),
+    ("pfast_server_submit", _i, [_p, _p, _p]),
+    ("pfast_server_wait", _i, [_p, C.c_longlong, _p]),
+    ("pfast_server_stats_get", _i, [_p, _p]),
 ]
 PFAST_NOALLOC_MAX_NODES = 1048576
 

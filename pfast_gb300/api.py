@@ -21,8 +21,8 @@ from . import _capi
 from ._capi import PFAST_MIXED, PFAST_PLAIN_FP64, PfastError, check, lib
 
 __all__ = ["fsm3d", "adjoint_fsm3d", "RT_fsm2d", "Tadjoint_fsm2d", "Radjoint_fsm2d", "Context", "Survey3D",
-           "Survey2D", "eval3d_host", "forward3d_host", "Inversion", "invert_options", "PfastError", "PFAST_PLAIN_FP64",
-           "PFAST_MIXED"]
+           "Survey2D", "eval3d_host", "forward3d_host", "Inversion", "invert_options", "Server", "Ticket", "PfastError",
+           "PFAST_PLAIN_FP64", "PFAST_MIXED"]
 
 
 def _arr(a, dtype, name, writable=False):
@@ -400,3 +400,129 @@ class Inversion:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------ request server
+class Server:
+    """Continuous-batching request server (pfast_server_*): models and surveys resident on the
+    device under IDs, forward and gradient requests of any size admitted against an HBM budget
+    and run `slots` at a time on their own streams.
+
+        srv = Server(device=0, slots=4, hbm_budget_gb=150)
+        srv.put_model(1, vp3d, (dx, dy, dz))             # 3D: vp [nz, nrows, ncols]
+        srv.put_survey3d(7, shape, spacing, src, srnum, rec, nxyz, tobs)
+        t = srv.submit_gradient(1, 7)                     # returns a Ticket
+        grad, misfit, info = t.result()
+    """
+
+    def __init__(self, device=0, slots=4, hbm_budget_gb=150.0, max_bypass=8):
+        cfg = _capi.ServerConfig(device=device, slots=slots, hbm_budget_bytes=float(hbm_budget_gb) * 1e9,
+                                 max_bypass=max_bypass)
+        self._h = C.c_void_p()
+        check(lib().pfast_server_create(C.byref(cfg), C.byref(self._h)), "server_create")
+        self._shapes = {}     # model id -> (dim, shape); survey id -> (dim, nrec, numofr)
+        self._surveys = {}
+
+    def put_model(self, model_id, vp, spacing, WR=None):
+        vp = np.ascontiguousarray(vp, np.float64)
+        dim = vp.ndim
+        if dim == 3:
+            nz, nr, nc = vp.shape
+            dx, dy, dz = spacing
+        else:
+            nr, nc = vp.shape
+            nz = 1
+            dx, dz = spacing
+            dy = 0.0
+        wr = None if WR is None else np.ascontiguousarray(np.broadcast_to(np.asarray(WR, np.float64), vp.shape))
+        check(lib().pfast_server_put_model(self._h, int(model_id), dim, nr, nc, nz, dx, dy, dz, vp.ctypes.data,
+                                           wr.ctypes.data if wr is not None else None), "server_put_model")
+        self._shapes[int(model_id)] = (dim, vp.shape)
+
+    def put_survey3d(self, survey_id, shape, spacing, src, srnum, rec, nxyz=None, tobs=None):
+        nz, nr, nc = shape
+        dx, dy, dz = spacing
+        a = [np.ascontiguousarray(src, np.int32), np.ascontiguousarray(srnum, np.int32),
+             np.ascontiguousarray(rec, np.int32)]
+        nx = None if nxyz is None else np.ascontiguousarray(nxyz, np.float64)
+        tx = None if tobs is None else np.ascontiguousarray(tobs, np.float64)
+        check(lib().pfast_server_put_survey3d(self._h, int(survey_id), nr, nc, nz, dx, dy, dz, len(a[1]),
+                                              a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data,
+                                              nx.ctypes.data if nx is not None else None,
+                                              tx.ctypes.data if tx is not None else None), "server_put_survey3d")
+        self._surveys[int(survey_id)] = (3, int(a[1].sum()), 0)
+
+    def put_survey2d(self, survey_id, shape, spacing, src, srnum, rec, numofr=0, Z=None, nxy=None, tt_obs=None,
+                     tr_obs=None):
+        nr, nc = shape
+        dx, dz = spacing
+        src = np.ascontiguousarray(src, np.int32)
+        srnum = np.ascontiguousarray(srnum, np.int32)
+        rec = np.ascontiguousarray(rec, np.int32)
+        ptr = lambda x: None if x is None else x.ctypes.data
+        Zc = np.ascontiguousarray(Z, np.float64) if (Z is not None and numofr) else None
+        nx = None if nxy is None else np.ascontiguousarray(nxy, np.float64)
+        tt = None if tt_obs is None else np.ascontiguousarray(tt_obs, np.float64)
+        tr = np.ascontiguousarray(tr_obs, np.float64) if (tr_obs is not None and numofr) else None
+        check(lib().pfast_server_put_survey2d(self._h, int(survey_id), nr, nc, dx, dz, len(srnum), ptr(src), ptr(srnum),
+                                              len(rec), ptr(rec), ptr(nx), ptr(tt), numofr, ptr(tr), ptr(Zc)),
+              "server_put_survey2d")
+        self._surveys[int(survey_id)] = (2, len(rec), numofr)
+
+    def drop_model(self, model_id):
+        check(lib().pfast_server_drop(self._h, 0, int(model_id)), "server_drop")
+
+    def drop_survey(self, survey_id):
+        check(lib().pfast_server_drop(self._h, 1, int(survey_id)), "server_drop")
+
+    def _submit(self, kind, model_id, survey_id, precision, maxswp, polish_floor, out):
+        dim, shape = self._shapes.get(int(model_id), (3, None))   # unknown IDs: the library rejects them
+        req = _capi.Request(kind=kind, model_id=int(model_id), survey_id=int(survey_id))
+        req.opt = _opts(precision, maxswp if maxswp else (100 if dim == 3 else 500), 0, polish_floor)
+        misfit = np.zeros(1)
+        req.out = out.ctypes.data
+        req.out_misfit = misfit.ctypes.data
+        t = C.c_longlong()
+        check(lib().pfast_server_submit(self._h, C.byref(req), C.byref(t)), "server_submit")
+        return Ticket(self, t.value, kind, out, misfit)
+
+    def submit_forward(self, model_id, survey_id, precision=PFAST_MIXED, maxswp=0, polish_floor=0.0):
+        dim, nrec, numofr = self._surveys.get(int(survey_id), (3, 1, 0))
+        out = np.empty((max(nrec, 1), numofr + 1) if dim == 2 else max(nrec, 1))
+        return self._submit(_capi.PFAST_REQ_FORWARD, model_id, survey_id, precision, maxswp, polish_floor, out)
+
+    def submit_gradient(self, model_id, survey_id, precision=PFAST_MIXED, maxswp=0, polish_floor=0.0):
+        out = np.empty(self._shapes.get(int(model_id), (3, (1,)))[1])
+        return self._submit(_capi.PFAST_REQ_GRADIENT, model_id, survey_id, precision, maxswp, polish_floor, out)
+
+    def stats(self):
+        st = _capi.ServerStats()
+        check(lib().pfast_server_stats_get(self._h, C.byref(st)), "server_stats")
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().pfast_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ticket:
+    """A submitted request; result() blocks until it is done and returns (output, misfit, info)."""
+
+    def __init__(self, server, ticket, kind, out, misfit):
+        self.server, self.ticket, self.kind, self._out, self._misfit = server, ticket, kind, out, misfit
+        self._res = None
+
+    def result(self):
+        if self._res is None:
+            r = _capi.RequestResult()
+            st = lib().pfast_server_wait(self.server._h, self.ticket, C.byref(r))
+            self._res = r.as_dict()
+            check(st, "server request")
+        return self._out, (float(self._misfit[0]) if self.kind == _capi.PFAST_REQ_GRADIENT else None), self._res

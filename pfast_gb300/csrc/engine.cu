@@ -38,10 +38,10 @@ pfast_status cuda_fail(cudaError_t e, const char* what, const char* file, int li
 // ------------------------------------------------------------------ buffers
 pfast_status DevBuf::ensure(size_t bytes) {
     if (bytes <= cap) return PFAST_OK;
-    if (p) cudaDeviceSynchronize();   // queued kernels may still use the old allocation
+    if (p && !astream) cudaDeviceSynchronize();   // queued kernels may still use the old allocation
     release();
     size_t want = std::max<size_t>(bytes, 256);
-    cudaError_t e = cudaMalloc(&p, want);
+    cudaError_t e = astream ? cudaMallocAsync(&p, want, astream) : cudaMalloc(&p, want);
     if (e != cudaSuccess) {
         p = nullptr;
         cap = 0;
@@ -54,14 +54,20 @@ pfast_status DevBuf::ensure(size_t bytes) {
 }
 
 void DevBuf::release() {
-    if (p) cudaFree(p);
+    if (p) {
+        if (astream) cudaFreeAsync(p, astream);
+        else cudaFree(p);
+    }
     p = nullptr;
     cap = 0;
 }
 
 pfast_status HostBuf::ensure(size_t bytes) {
     if (bytes <= cap) return PFAST_OK;
-    if (p) cudaDeviceSynchronize();   // an async copy may still read or write the old buffer
+    if (p) {   // an async copy may still read or write the old buffer
+        if (sstream) cudaStreamSynchronize(sstream);
+        else cudaDeviceSynchronize();
+    }
     release();
     size_t want = std::max<size_t>(bytes, 4096);
     PFAST_CUDA_TRY(cudaMallocHost(&p, want));
@@ -73,6 +79,22 @@ void HostBuf::release() {
     if (p) cudaFreeHost(p);
     p = nullptr;
     cap = 0;
+}
+
+std::vector<DevBuf*> ctx_buffers(pfast_ctx* ctx) {
+    return {&ctx->s64,  &ctx->s32,  &ctx->sq64,     &ctx->T32,    &ctx->tflags,    &ctx->T64,   &ctx->L64,
+            &ctx->scratch, &ctx->mask, &ctx->act,  &ctx->changed, &ctx->ee,     &ctx->need,    &ctx->misc,
+            &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a, &ctx->f2b, &ctx->f2c, &ctx->work,
+            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c};
+}
+
+void ctx_release_buffers(pfast_ctx* ctx) {
+    for (DevBuf* b : ctx_buffers(ctx)) b->release();
+}
+
+void ctx_stream_ordered(pfast_ctx* ctx) {
+    for (DevBuf* b : ctx_buffers(ctx)) b->astream = ctx->own_stream;
+    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work}) b->sstream = ctx->own_stream;
 }
 
 void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc) {
@@ -556,10 +578,7 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
     if (!ctx) return PFAST_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->s64, &ctx->s32, &ctx->sq64, &ctx->T32, &ctx->tflags, &ctx->T64, &ctx->L64, &ctx->scratch, &ctx->mask, &ctx->act, &ctx->changed,
-                      &ctx->ee, &ctx->need, &ctx->misc, &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a,
-                      &ctx->f2b, &ctx->f2c, &ctx->work, &ctx->queue})
-        b->release();
+    pfast::ctx_release_buffers(ctx);
     for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work}) b->release();
     for (auto& kv : ctx->diag3) free_diag_table3(kv.second);
     for (auto& kv : ctx->diag2) free_diag_table2(kv.second);

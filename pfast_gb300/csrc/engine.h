@@ -12,19 +12,24 @@
 
 namespace pfast {
 
-// Grow-only device buffer.
+// Grow-only device buffer.  With `astream` set (contexts of the request server) the buffer
+// is allocated and freed stream-ordered on that stream, so growing or releasing it never
+// synchronises the device (other slots' work keeps running).
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
+    cudaStream_t astream = nullptr;
     pfast_status ensure(size_t bytes);
     void release();
     template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
-// Pinned host scratch for per-iteration flags and lists.
+// Pinned host scratch for per-iteration flags and lists.  With `sstream` set, growing waits
+// for that stream only (its context's copies) instead of the whole device.
 struct HostBuf {
     void* p = nullptr;
     size_t cap = 0;
+    cudaStream_t sstream = nullptr;
     pfast_status ensure(size_t bytes);
     void release();
     template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
@@ -46,6 +51,7 @@ struct pfast_ctx {
     pfast::HostBuf h_act, h_changed, h_ee, h_need, h_work;
     pfast::DevBuf work;                 // executed node updates per instance (sweep kernels)
     pfast::DevBuf queue;                // work counter of the persistent sweep kernel
+    pfast::DevBuf out_a, out_b, out_c;  // request server: device outputs of a request
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
     std::map<std::pair<int, int>, pfast::DiagTable2> diag2;
     cudaEvent_t ev[8] = {};
@@ -113,6 +119,12 @@ pfast_status default_context(pfast_ctx** out);
 // Slowness arrays of a model (s64 always; s32 and s^2 for the mixed mode); rejects a
 // model with a non-positive or non-finite velocity.
 pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed);
+
+// Every device buffer of a context; release them all (stream-ordered for server contexts);
+// make a context's buffers stream-ordered on its own stream (request server slots).
+std::vector<DevBuf*> ctx_buffers(pfast_ctx* ctx);
+void ctx_release_buffers(pfast_ctx* ctx);
+void ctx_stream_ordered(pfast_ctx* ctx);
 
 // Time between two recorded events, added to *acc (ms).
 void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc);
