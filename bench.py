@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--plain-sources", type=int, default=32)
     p.add_argument("--cpu-sample", type=int, default=0, help="sources per CPU sample (0 = one per host thread)")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the secondary workloads (2D inversion, batched uneven 3D models, serving stream)")
     return p.parse_args()
 
 
@@ -146,6 +148,37 @@ def run_reference(args, rank):
                              "sample": f"{ns} sources x 1 evaluation per step on {nthreads} threads, scaled to 256 sources"},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def extras():
+    """Secondary workloads, each reported beside the headline (bounded: about two minutes in all):
+    the 2D joint inversion (15 L-BFGS iterations, mixed vs plain FP64), 48 uneven 3D models
+    batched through the request server vs sequential plain FP64 (plain timed on 12 models and
+    scaled), and a Poisson serving stream at two offered loads (mixed) and one (plain)."""
+    out = {}
+    jobs = (("inversion_2d", lambda: __import__("pfast_gb300.inv_bench", fromlist=["run"]).run(15)),
+            ("batched_uneven_3d", lambda: {k: v for k, v in __import__("pfast_gb300.batch_bench", fromlist=["run"])
+                                           .run(48, 8, plain_models=12).items() if k not in ("shapes", "sources")}),
+            ("serving", serving))
+    for key, fn in jobs:
+        try:
+            out[key] = fn()
+        except Exception as e:   # a secondary workload must not cost the headline line
+            out[key] = {"error": repr(e)[:400]}
+    return out
+
+
+def serving():
+    import pfast_gb300 as pg
+    from pfast_gb300 import serve_bench
+    rng = np.random.default_rng(5)
+    pool = serve_bench.model_pool(rng)
+    res = {"mixed": serve_bench.sweep([4.0, 16.0], 8.0, pg.PFAST_MIXED, pool=pool),
+           "plain": serve_bench.sweep([4.0], 8.0, pg.PFAST_PLAIN_FP64, pool=pool),
+           "workload": "Poisson arrivals, 70% forward / 30% gradient, 2D 201x201..1001x401 (1 reflector) and 3D "
+                       "64^3..256x256x128 grids log-uniform, 1-64 sources, 50% resident-model reuse, 8 slots, "
+                       "150 GB budget; latency from arrival to host result"}
+    return res
 
 
 def main():
@@ -271,6 +304,7 @@ def main():
         cpu = {"value": cv, "unit": "evals/s", "cores": nthreads, "kind": "port",
                "sample": f"{ns} of 256 sources, one misfit+gradient evaluation ({cdt:.1f} s), scaled to 256 sources"}
 
+    line = None
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -294,9 +328,12 @@ def main():
                 "step_ms": step_ms,
                 "phase_ms": {k: st[k] for k in ("ms_fwd32", "ms_fwd64", "ms_adj32", "ms_adj64", "ms_other", "ms_total")},
                 "iters": {k: st[k] for k in ("fwd32_iters_max", "fwd_iters_max", "adj32_iters_max", "adj_iters_max")}}
-        print(json.dumps(line), flush=True)
     sv.close()
     ctx.close()
+    if rank == 0:
+        if world == 1 and not args.no_extras:
+            line["extras"] = extras()
+        print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 
