@@ -53,6 +53,11 @@ typedef struct {
     int schedule;         /* 3D sweeps: 0 = automatic, 1 = one launch per tile diagonal (every tile of
                              every source spread over all SMs), 2 = persistent (one block solves one
                              source; automatic picks it from 4 sources per SM).  Same results. */
+    int near_source_radius;  /* 3D forward, opt-in (not in the reference): nodes within this many grid
+                             nodes of the source (Euclidean, in nodes) start from the straight-ray
+                             traveltime 0.5*(s_src + s_node)*distance and stay fixed, which removes most
+                             of the first-order scheme's source error.  0 = off (the reference's
+                             point-source start; results bit-identical to it). */
 } pfast_options;
 #define PFAST_SCHEDULE_AUTO 0
 #define PFAST_SCHEDULE_DIAGONAL 1

@@ -26,7 +26,7 @@ PFAST_SCHEDULE_AUTO, PFAST_SCHEDULE_DIAGONAL, PFAST_SCHEDULE_PERSISTENT = 0, 1, 
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int), ("polish_floor", C.c_double),
-                ("schedule", C.c_int)]
+                ("schedule", C.c_int), ("near_source_radius", C.c_int)]
 
 
 class Stats(C.Structure):

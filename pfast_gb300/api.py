@@ -88,13 +88,14 @@ def Radjoint_fsm2d(UR, Td, Tu, TR_obs, rec, nxyz, src, srnum, srcid, NumofR, MAX
 
 
 # ------------------------------------------------------------ batched layer
-def _opts(precision, maxswp, max_batch, polish_floor=0.0, schedule=0):
+def _opts(precision, maxswp, max_batch, polish_floor=0.0, schedule=0, near_source_radius=0):
     o = _capi.Options()
     o.precision = int(precision)
     o.maxswp = int(maxswp)
     o.max_batch = int(max_batch)
     o.polish_floor = float(polish_floor)
     o.schedule = int(schedule)
+    o.near_source_radius = int(near_source_radius)
     return o
 
 
@@ -167,7 +168,8 @@ class Survey3D:
                                           tx.ctypes.data if tx is not None else None, C.byref(self._h)),
               "survey3d_create")
 
-    def eval(self, vp, grad=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0, polish_floor=0.0, schedule=0):
+    def eval(self, vp, grad=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0, polish_floor=0.0, schedule=0,
+             near_source_radius=0):
         """Misfit + gradient for the device model vp (torch float64 [nz, nrows, ncols]).
         Returns (grad tensor, misfit, stats dict)."""
         import torch
@@ -176,20 +178,20 @@ class Survey3D:
             grad = torch.empty(self.shape, dtype=torch.float64, device=vp.device)
         E = C.c_double(0)
         st = _capi.Stats()
-        o = _opts(precision, maxswp, max_batch, polish_floor, schedule)
+        o = _opts(precision, maxswp, max_batch, polish_floor, schedule, near_source_radius)
         check(lib().pfast_survey3d_eval(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
                                         _dev_ptr(grad, "grad", numel=n), C.addressof(E), C.byref(st)), "survey3d_eval")
         return grad, E.value, st.as_dict()
 
     def forward(self, vp, picks=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0, polish_floor=0.0,
-                schedule=0):
+                schedule=0, near_source_radius=0):
         """First-arrival picks [sum(srnum)] for the device model vp.  Returns (picks, stats)."""
         import torch
         n = int(np.prod(self.shape))
         if picks is None:
             picks = torch.empty(max(self.nrec, 1), dtype=torch.float64, device=vp.device)
         st = _capi.Stats()
-        o = _opts(precision, maxswp, max_batch, polish_floor, schedule)
+        o = _opts(precision, maxswp, max_batch, polish_floor, schedule, near_source_radius)
         check(lib().pfast_survey3d_forward(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
                                            _dev_ptr(picks, "picks", numel=self.nrec), C.byref(st)), "survey3d_forward")
         return picks[:self.nrec], st.as_dict()

@@ -265,6 +265,7 @@ Sweep3Args base_args(const pfast_survey3d* sv) {
     a.sp = make_spacing(sv->dx, sv->dy, sv->dz);
     a.wpr = (sv->nc + 31) / 32;
     a.polish_floor = kPolishFloor;
+    a.src_r2 = 0;
     return a;
 }
 
@@ -302,12 +303,16 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     Sweep3Args a = base_args(sv);
     a.fstride = N;
     a.src_kij = sv->d_src_kij + 3 * b0;
+    a.src_r2 = ctx->near_radius * ctx->near_radius;
     const long long* src_lin = sv->d_src_lin + b0;
     int dummy_nc = 0;
     int* nc_ptr = st ? &st->not_converged : &dummy_nc;
     long long* nu = st ? &st->fwd_node_updates : nullptr;
     if (precision == PFAST_PLAIN_FP64) {
         PFAST_LAUNCH(ctx, launch_init_fwd3(ctx->T64.p, 0, N, N, src_lin, nb, s));
+        if (ctx->near_radius > 0)
+            PFAST_LAUNCH(ctx, launch_near_source3(ctx->T64.p, 0, N, a.src_kij, ctx->s64.as<double>(), sv->nz, sv->nr,
+                                                  sv->nc, a.sp, ctx->near_radius, nb, s));
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = ctx->T64.p;
         a.snap = ctx->scratch.p;
@@ -325,6 +330,9 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         float* T32 = ctx->scratch.as<float>();
         float* snap32 = T32 + N * nb;
         PFAST_LAUNCH(ctx, launch_init_fwd3(T32, 1, N, N, src_lin, nb, s));
+        if (ctx->near_radius > 0)
+            PFAST_LAUNCH(ctx, launch_near_source3(T32, 1, N, a.src_kij, ctx->s64.as<double>(), sv->nz, sv->nr, sv->nc,
+                                                  a.sp, ctx->near_radius, nb, s));
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = T32;
         a.snap = snap32;
@@ -335,6 +343,9 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
                               st ? &st->ms_fwd32 : nullptr));
         if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
         PFAST_LAUNCH(ctx, launch_widen(T32, ctx->T64.as<double>(), N, N, N, nb, s));
+        if (ctx->near_radius > 0)   // the fixed region keeps its FP64 values in the polish
+            PFAST_LAUNCH(ctx, launch_near_source3(ctx->T64.p, 0, N, a.src_kij, ctx->s64.as<double>(), sv->nz, sv->nr,
+                                                  sv->nc, a.sp, ctx->near_radius, nb, s));
         std::fill(iters.begin(), iters.end(), 0);
         active.resize(nb);
         for (int b = 0; b < nb; ++b) active[b] = b;
@@ -483,6 +494,10 @@ bool valid_options(const pfast_options* opt) {
         set_last_error("unknown schedule %d", opt->schedule);
         return false;
     }
+    if (opt->near_source_radius < 0 || opt->near_source_radius > 64) {
+        set_last_error("near_source_radius must be in [0, 64]");
+        return false;
+    }
     return true;
 }
 
@@ -493,6 +508,7 @@ pfast_options resolve(const pfast_options* opt, int default_maxswp) {
     o.max_batch = 0;
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
+    o.near_source_radius = 0;
     if (opt) o = *opt;
     return o;
 }
@@ -548,6 +564,7 @@ void pfast_default_options(pfast_options* opt) {
     opt->max_batch = 0;
     opt->polish_floor = 0.0;
     opt->schedule = PFAST_SCHEDULE_AUTO;
+    opt->near_source_radius = 0;
 }
 
 pfast_status pfast_ctx_create(int device, pfast_ctx** out) {
@@ -701,6 +718,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     pfast_options o = resolve(opt, 100);
     ctx->polish_floor = o.polish_floor > 0.0 ? (float)o.polish_floor : kPolishFloor;
     ctx->schedule = o.schedule;
+    ctx->near_radius = o.near_source_radius;
     stats_begin(stats);
     PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
@@ -836,6 +854,7 @@ pfast_status pfast_fsm3d(double* vp, double* U, int* src, int srcid, int MAXSwp,
     }
     if (!r) r = prepare_slowness(ctx, ctx->vp_tmp.as<double>(), N, false);
     ctx->schedule = PFAST_SCHEDULE_AUTO;
+    ctx->near_radius = 0;
     if (!r) r = forward3d_batch(ctx, sv, 0, 1, PFAST_PLAIN_FP64, MAXSwp, nullptr);
     if (!r) {
         cudaError_t e = cudaMemcpyAsync(U, ctx->T64.p, sizeof(double) * N, cudaMemcpyDeviceToHost, s);

@@ -58,6 +58,7 @@ struct pfast_ctx {
     long long launches = 0;
     float polish_floor = pfast::kPolishFloor;   // of the current 3D evaluation (pfast_options)
     int schedule = PFAST_SCHEDULE_AUTO;         // of the current 3D evaluation (pfast_options)
+    int near_radius = 0;                        // of the current 3D evaluation (pfast_options)
 };
 
 struct pfast_survey3d {

@@ -497,6 +497,7 @@ pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp
     o.max_batch = 0;
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
+    o.near_source_radius = 0;
     if (opt) o = *opt;
     if (st) std::memset(st, 0, sizeof(*st));
     if (sv->geom_status) {
@@ -554,6 +555,7 @@ pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, c
     o.max_batch = 0;
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
+    o.near_source_radius = 0;
     if (opt) o = *opt;
     if (st) std::memset(st, 0, sizeof(*st));
     if (!sv->has_picks) { set_last_error("survey has no picks: gradient unavailable"); return PFAST_ERR_INVALID; }
@@ -810,6 +812,7 @@ pfast_status pfast_RT_fsm2d(double* vp, double* U, double* TTd, double* TTu, dou
     o.max_batch = 1;
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
+    o.near_source_radius = 0;
     if (!r) r = forward2d_impl(ctx, sv, ctx->vp_tmp.as<double>(), &o, nullptr, TTd, TTu, U, nullptr);
     pfast_survey2d_destroy(sv);
     return r;

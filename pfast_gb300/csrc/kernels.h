@@ -20,6 +20,8 @@ struct Sweep3Args {
     long long mask_stride;
     int wpr;                  // mask words per grid row
     const int* src_kij;       // forward: per-instance source node (k, i, j)
+    int src_r2;               // forward: nodes with squared node distance <= src_r2 from the source are
+                              // fixed (0: the source node only, the reference's point source)
     void* snap;               // per-instance snapshot of the iteration start (Real)
     int* changed;             // per-instance "an update exceeded the tolerance" flag
     const int* act;           // active instance ids; grid.y indexes it
@@ -72,6 +74,10 @@ pfast_status persistent_shape(int kind, int nact, int* warps, int* blocks);
 // when some vp is not a positive finite number.
 pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, int* bad, long long n,
                              cudaStream_t st);
+// Opt-in near-source start: nodes within `radius` nodes (Euclidean) of each instance's source get
+// 0.5*(s_src + s_node)*distance.  field: FP32 (is_fp32) or FP64 fields, fstride apart.
+pfast_status launch_near_source3(void* field, int is_fp32, long long fstride, const int* src_kij, const double* s64,
+                                 int nz, int nr, int nc, const Spacing3& sp, int radius, int nb, cudaStream_t st);
 pfast_status launch_init_fwd3(void* field, int is_fp32, long long fstride, long long n, const long long* src_lin,
                               int nbatch, cudaStream_t st);
 pfast_status launch_widen(const float* src, double* dst, long long fstride32, long long fstride64, long long n,

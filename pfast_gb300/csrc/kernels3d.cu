@@ -412,7 +412,8 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             const Real old = box[c];
             Real nv = old;
             if constexpr (!ADJ) {
-                if (!(gk == sk && gi == si && gj == sj)) {
+                const int qk = gk - sk, qi = gi - si, qj = gj - sj;
+                if (qk * qk + qi * qi + qj * qj > A.src_r2) {   // the source node (and the opt-in fixed region) stays
                     const Aux s = __ldg(reinterpret_cast<const Aux*>(A.aux) + rowbase + gj);
                     if constexpr (KIND == kFwdPlain64) {
                         const double xa = min_nonneg(box[c + 1], box[c - 1]);
@@ -849,6 +850,28 @@ __global__ void init_fwd_kernel(Real* __restrict__ f, long long fstride, long lo
         g[t] = (t == sn) ? Real(0) : Real(kInf);   // point-source initialisation, src/T_pfsm3d.h:139-148
 }
 
+// Near-source start (opt-in): block y = instance, threads over the (2r+1)^3 cube.
+template <typename Real>
+__global__ void near_source_kernel(Real* __restrict__ f, long long fstride, const int* __restrict__ src_kij,
+                                   const double* __restrict__ s64, int nz, int nr, int nc, double dx, double dy,
+                                   double dz, int r) {
+    const int b = blockIdx.y;
+    const int sk = src_kij[3 * b], si = src_kij[3 * b + 1], sj = src_kij[3 * b + 2];
+    const int w = 2 * r + 1;
+    const long long plane = (long long)nr * nc;
+    const double ss = s64[sk * plane + (long long)si * nc + sj];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w * w * w; t += gridDim.x * blockDim.x) {
+        const int qk = t / (w * w) - r, qi = (t / w) % w - r, qj = t % w - r;
+        const int k = sk + qk, i = si + qi, j = sj + qj;
+        if (k < 0 || k >= nz || i < 0 || i >= nr || j < 0 || j >= nc) continue;
+        if (qk * qk + qi * qi + qj * qj > r * r) continue;
+        const long long node = k * plane + (long long)i * nc + j;
+        const double ex = qj * dx, ey = qi * dy, ez = qk * dz;
+        const double dist = sqrt(ex * ex + ey * ey + ez * ez);
+        f[b * fstride + node] = Real(0.5 * (ss + s64[node]) * dist);
+    }
+}
+
 __global__ void widen_kernel(const float* __restrict__ a, double* __restrict__ b, long long s32, long long s64, long long n) {
     const int k = blockIdx.y;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
@@ -958,6 +981,22 @@ pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* 
                              cudaStream_t st) {
     slowness_kernel<<<grid_for(n), kThreads, 0, st>>>(vp, s64, s32, sq64, bad, n);
     PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_near_source3(void* field, int is_fp32, long long fstride, const int* src_kij, const double* s64,
+                                 int nz, int nr, int nc, const Spacing3& sp, int radius, int nb, cudaStream_t st) {
+    if (radius <= 0 || nb <= 0) return PFAST_OK;
+    const int w = 2 * radius + 1;
+    dim3 grid((unsigned)((w * w * w + kThreads - 1) / kThreads), nb);
+    if (is_fp32)
+        near_source_kernel<float><<<grid, kThreads, 0, st>>>((float*)field, fstride, src_kij, s64, nz, nr, nc, sp.d[0],
+                                                             sp.d[1], sp.d[2], radius);
+    else
+        near_source_kernel<double><<<grid, kThreads, 0, st>>>((double*)field, fstride, src_kij, s64, nz, nr, nc,
+                                                              sp.d[0], sp.d[1], sp.d[2], radius);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "near_source launch", __FILE__, __LINE__);
     return PFAST_OK;
 }
 
