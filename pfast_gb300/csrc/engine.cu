@@ -187,6 +187,13 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     a.work = ctx->work.as<unsigned long long>();
     PFAST_CUDA_TRY(cudaMemsetAsync(a.work, 0, sizeof(unsigned long long) * nb, st));
     PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * nb, st));
+    if ((kind == kFwdPolish64 || kind == kAdjPolish64) && !active.empty()) {
+        // initial selected orders per tile, so the first polish sweep skips unselected tiles
+        const int nact0 = (int)active.size();
+        std::memcpy(h_act, active.data(), sizeof(int) * nact0);
+        PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact0, cudaMemcpyHostToDevice, st));
+        PFAST_LAUNCH(ctx, launch_polish_orders3(kind, a, nb, nact0, st));
+    }
     // Two schedules.  Per-diagonal launches spread every tile of every active instance over
     // all SMs (one warp per tile) and suit surveys with few instances per SM, such as 256
     // sources on 152 SMs; the persistent kernel (one block solves one instance, no host

@@ -59,6 +59,9 @@ void free_diag_table3(DiagTable3& t);
 size_t sweep3_smem_bytes(int kind);
 // changed[act[b]] = any diff over the tiles of instance act[b], b < nact.
 pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
+// Polish kinds: initial lock words (every order due, the tile's selected orders in bits 8-15),
+// computed from a.field (forward) or a.aux (adjoint) for the nb instances (a.act lists nact).
+pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int nact, cudaStream_t st);
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
 // Persistent sweep kernel: `blocks` blocks of `warps` warps take the nact instances of a.act
 // from *queue (zeroed by the caller) and solve each to convergence (maxiter outer

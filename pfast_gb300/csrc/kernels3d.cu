@@ -632,6 +632,53 @@ __global__ void __launch_bounds__(kMaxPWarps * 32) sweep3d_persistent(const Swee
     }
 }
 
+// Polish pre-pass: lock word of every tile = all eight orders due | (orders in which some node
+// of the tile is selected) << 8, the selection computed from the field the polish starts
+// from (forward: the widened bulk traveltimes; adjoint: the fixed traveltimes), so that the
+// first polish sweep skips the tiles none of whose nodes it selects.  One thread per node;
+// the lanes of a warp that share a tile OR their masks and one of them ORs it in.
+template <bool ADJ>
+__global__ void tile_orders_kernel(const Sweep3Args A) {
+    const int inst = A.act[blockIdx.y];
+    const int nz = A.nz, nr = A.nr, nc = A.nc;
+    const long long plane = (long long)nr * nc, N = plane * nz;
+    const double* f = reinterpret_cast<const double*>(ADJ ? A.aux : A.field) + inst * A.fstride;
+    const int lane = threadIdx.x & 31;
+    int sk = 0, si = 0, sj = 0;
+    if (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
+    const long long inf = dbits(INFINITY);
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x - lane); base < N; base += step) {
+        const long long t = base + lane;
+        const bool valid = t < N;
+        unsigned m = 0;
+        int tid = -1;
+        if (valid) {
+            const int k = (int)(t / plane), i = (int)((t / nc) % nr), j = (int)(t % nc);
+            tid = ((k / TK) * A.nbi + i / TI) * A.nbj + j / TJ;
+            const long long xl = j > 0 ? dbits(f[t - 1]) : inf, xh = j < nc - 1 ? dbits(f[t + 1]) : inf;
+            const long long yl = i > 0 ? dbits(f[t - nc]) : inf, yh = i < nr - 1 ? dbits(f[t + nc]) : inf;
+            const long long zl = k > 0 ? dbits(f[t - plane]) : inf, zh = k < nz - 1 ? dbits(f[t + plane]) : inf;
+            if constexpr (ADJ) {
+                const bool interior = k >= 1 && k <= nz - 2 && i >= 1 && i <= nr - 2 && j >= 1 && j <= nc - 2;
+                const bool fixed = (A.mask[inst * A.mask_stride + ((long long)k * nr + i) * A.wpr + (j >> 5)] >> (j & 31)) & 1u;
+                if (interior && !fixed) m = adj_orders(dbits(f[t]), xl, xh, yl, yh, zl, zh);
+            } else {
+                const int qk = k - sk, qi = i - si, qj = j - sj;
+                if (qk * qk + qi * qi + qj * qj > A.src_r2) m = fwd_orders(dbits(f[t]), xl, xh, yl, yh, zl, zh);
+            }
+        }
+        const unsigned grp = __match_any_sync(0xffffffffu, tid);
+        const unsigned om = __reduce_or_sync(grp, m);
+        if (valid && om && lane == __ffs(grp) - 1) atomicOr(A.dirty + (long long)inst * A.ntiles + tid, (int)(om << 8));
+    }
+}
+
+__global__ void fill_int_kernel(int* __restrict__ p, long long n, int v) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        p[t] = v;
+}
+
 // changed[act[b]] = OR over the tiles of instance act[b] of diff.
 __global__ void reduce_diff_kernel(const int* __restrict__ diff, int ntiles, const int* __restrict__ act,
                                    int* __restrict__ changed) {
@@ -795,6 +842,19 @@ pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, i
     }
     set_last_error("unknown sweep kind %d", kind);
     return PFAST_ERR_INVALID;
+}
+
+pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int nact, cudaStream_t st) {
+    if (nact <= 0) return PFAST_OK;
+    const long long n = (long long)a.ntiles * nb;
+    fill_int_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 32), 256, 0, st>>>(a.dirty, n, 0xff);
+    const long long N = (long long)a.nz * a.nr * a.nc;
+    dim3 grid((unsigned)std::min<long long>((N + 255) / 256, 152LL * 8), nact);
+    if (kind == kAdjPolish64) tile_orders_kernel<true><<<grid, 256, 0, st>>>(a);
+    else tile_orders_kernel<false><<<grid, 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "polish orders launch", __FILE__, __LINE__);
+    return PFAST_OK;
 }
 
 pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st) {
