@@ -100,26 +100,39 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
             if (caps[q] > 0) keep.push_back(q);
         active.swap(keep);
     }
+    // tile-locking flags (see the 3D sweeps): every tile unlocked, no snapshot yet
+    const long long ntiles = (long long)dt.nbi * dt.nbj;
+    PFAST_TRY2(ctx->tflags.ensure(sizeof(int) * 3 * ntiles * ninst));
+    a.ntiles = (int)ntiles;
+    a.dirty = ctx->tflags.as<int>();
+    a.stamp = a.dirty + ntiles * ninst;
+    a.diff = a.stamp + ntiles * ninst;
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0xff, sizeof(int) * ntiles * ninst, st));
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * ninst, st));
+    PFAST_TRY2(ctx->work.ensure(sizeof(unsigned long long) * ninst));
+    PFAST_TRY2(ctx->h_work.ensure(sizeof(unsigned long long) * ninst));
+    a.work = ctx->work.as<unsigned long long>();
+    PFAST_CUDA_TRY(cudaMemsetAsync(a.work, 0, sizeof(unsigned long long) * ninst, st));
     int it = 0;
     while (!active.empty()) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
-        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * ninst, st));
+        PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles * ninst, st));
+        a.iter = it;
         for (int dir = 0; dir < 4; ++dir) {
             a.dir = dir;
-            a.first = dir == 0;
-            a.last = dir == 3;
             for (int d = 0; d < dt.ndiag; ++d) {
                 PFAST_LAUNCH(ctx, launch_sweep2(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
             }
         }
+        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * ninst, st));
+        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.ntiles, a.act, nact, a.changed, st));
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) return cuda_fail(le, "sweep2 launch", __FILE__, __LINE__);
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * ninst, cudaMemcpyDeviceToHost, st));
         PFAST_CUDA_TRY(cudaStreamSynchronize(st));
         ++it;
-        if (node_updates) *node_updates += (long long)nact * 4 * nodes;
         std::vector<int> still;
         for (int q : active) {
             iters[q] = it;
@@ -129,6 +142,12 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
             }
         }
         active.swap(still);
+    }
+    if (node_updates) {
+        unsigned long long* hw = ctx->h_work.as<unsigned long long>();
+        PFAST_CUDA_TRY(cudaMemcpyAsync(hw, a.work, sizeof(unsigned long long) * ninst, cudaMemcpyDeviceToHost, st));
+        PFAST_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int q = 0; q < ninst; ++q) *node_updates += (long long)hw[q];
     }
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[5], st));
     add_elapsed(ctx->ev[4], ctx->ev[5], ms_acc);
@@ -144,6 +163,8 @@ Sweep2Args base2(const pfast_survey2d* sv) {
     a.dz = sv->dz;
     a.inv2x = 1.0 / sv->dx / sv->dx;
     a.inv2z = 1.0 / sv->dz / sv->dz;
+    a.dxf = (float)sv->dx;
+    a.dzf = (float)sv->dz;
     a.wpr = (sv->nc + 31) / 32;
     return a;
 }

@@ -109,7 +109,9 @@ __device__ __forceinline__ double adj2_polish(double T0, double Txp, double Txm,
     adj2_terms<double>(T0, Txp, Txm, Tzp, Tzm, Lxp, Lxm, Lzp, Lzm, wx, wz, num, den);
     if (!(fabs(den) > 1e-9)) return 0.0;
     const double r = fma(-den, L0, num);
-    return L0 + (double)__fdividef((float)r, (float)den);
+    const float step = __fdividef((float)r, (float)den);
+    // corrections far below the convergence tolerance are dropped (bitwise fixed point, tiles lock)
+    return fabsf(step) <= kPolishFloor * (1.0f + fabsf((float)L0)) ? L0 : L0 + (double)step;
 }
 
 // FP64 polish Godunov update, one Newton step on f(q) = wx max(q-a,0)^2 + wz max(q-b,0)^2 - s^2
@@ -120,7 +122,38 @@ __device__ __forceinline__ double eik2_newton(double U0, double a, double b, dou
     const double f = fma(wx * px, px, fma(wz * pz, pz, -s * s));
     const float fp = 2.0f * ((float)wx * (float)px + (float)wz * (float)pz);
     if (!(fp > 0.0f)) return fmin(fma(dx, s, a), fma(dz, s, b));
-    return U0 - (double)__fdividef((float)f, fp);
+    const float step = __fdividef((float)f, fp);
+    return fabsf(step) <= kPolishFloor ? U0 : U0 - (double)step;   // bitwise fixed point once converged
+}
+
+// Bitwise equality of two field values (FP32 or FP64).
+template <typename Real>
+__device__ __forceinline__ bool bits_same(Real a, Real b) {
+    if constexpr (sizeof(Real) == 8) return __double_as_longlong(a) == __double_as_longlong(b);
+    else return __float_as_uint(a) == __float_as_uint(b);
+}
+
+// ----------------------------------------------------------- quadrant selection (2D polish)
+// Sweep order o: bit 0 = columns ascending, bit 1 = rows ascending.  The 2D form of the 3D
+// octant selection: a polish update runs only in the orders that visit the node's active
+// upwind neighbours (forward) / its larger-traveltime neighbours (adjoint) first.
+constexpr unsigned kAscX2 = 0xa, kDescX2 = 0x5, kAscZ2 = 0xc, kDescZ2 = 0x3;
+
+__device__ __forceinline__ unsigned fwd_orders2(long long u, long long xlo, long long xhi, long long zlo,
+                                                long long zhi) {
+    unsigned m = 0xf;
+    if (u > (xlo < xhi ? xlo : xhi)) m &= xlo < xhi ? kAscX2 : (xhi < xlo ? kDescX2 : 0xfu);
+    if (u > (zlo < zhi ? zlo : zhi)) m &= zlo < zhi ? kAscZ2 : (zhi < zlo ? kDescZ2 : 0xfu);
+    return m;
+}
+
+__device__ __forceinline__ unsigned adj_orders2(long long t, long long xlo, long long xhi, long long zlo,
+                                                long long zhi) {
+    unsigned m = 0xf;
+    const bool a = xlo > t, b = xhi > t, c = zlo > t, e = zhi > t;
+    if (a != b) m &= a ? kAscX2 : kDescX2;
+    if (c != e) m &= c ? kAscZ2 : kDescZ2;
+    return m;
 }
 
 template <typename Dst, typename Src, typename Conv>
@@ -174,6 +207,20 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     const int bif = pk & 0xffff, bjf = pk >> 16;
     const int ti = py ? bif : A.nbi - 1 - bif;
     const int tj = px ? bjf : A.nbj - 1 - bjf;
+    // tile locking, as in the 3D sweeps: bits 0-3 = orders still to process, bits 4-7 (polish)
+    // = orders in which some node of the tile is selected
+    constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
+    const int tid = ti * A.nbj + tj;
+    int* dirty = A.dirty + (long long)q * A.ntiles;
+    const int dm = __ldcg(dirty + tid);
+    const int obit = 1 << A.dir;
+    const int omask = kSelective ? (dm >> 4) & 0xf : 0xf;
+    if (!(dm & omask & obit)) return;   // locked for this order (warp-uniform)
+    __syncwarp();
+    if (lane == 0) {
+        dirty[tid] = kSelective ? (dm & ~obit) : 0;
+        if (A.work) atomicAdd(A.work + q, (unsigned long long)(min(T2I, A.nr - ti * T2I) * min(T2J, A.nc - tj * T2J)));
+    }
     const int i0 = ti * T2I, j0 = tj * T2J;
     const int nr = A.nr, nc = A.nc;
     const int ei = min(T2I, nr - i0), ej = min(T2J, nc - j0);
@@ -209,9 +256,12 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
         }
     }
 
-    if (A.first) {
+    // snapshot at the tile's first processing in this outer iteration
+    int* stamp = A.stamp + (long long)q * A.ntiles;
+    if (__ldcg(stamp + tid) != A.iter) {
         for (int y = 0; y < ei; ++y)
             for (int x = lane; x < ej; x += 32) snp[(long long)(i0 + y) * nc + j0 + x] = box[(y + 1) * R2 + x + 1];
+        if (lane == 0) stamp[tid] = A.iter;
     }
     __syncwarp();
 
@@ -226,6 +276,8 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     const float rsum = float(1.0 / (A.inv2x + A.inv2z));
     const int cb = (li + 1) * R2 + 1;
     const int steps = ei + ej - 1;
+    bool chg = false, chg_jlo = false, chg_jhi = false;
+    unsigned sel = 0;
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
@@ -237,23 +289,35 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
             if constexpr (!ADJ) {
                 const bool upd = (rl == nullptr || gi <= __ldg(rl + gj)) && !(gi == si && gj == sj);
                 if (upd) {
+                    const Real old = box[c];
+                    Real nv = old;
                     const Real bz = ref_min(box[c - R2], box[c + R2]);
                     const Real ax = ref_min(box[c + 1], box[c - 1]);
                     const Real s = __ldg(slow + (long long)gi * nc + gj);
                     if constexpr (KIND == kFwdPlain64) {
                         const double qv = eik2_plain(ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z);
-                        box[c] = ref_min(box[c], qv);
+                        nv = ref_min(old, qv);
                     } else if constexpr (KIND == kFwdFast32) {
-                        const float qv = eik2_fast<float>(ax, bz, s, (float)A.dx, (float)A.dz, wx, wz, rsum);
-                        box[c] = ref_min(box[c], qv);
+                        const float qv = eik2_fast<float>(ax, bz, s, A.dxf, A.dzf, wx, wz, rsum);
+                        nv = ref_min(old, qv);
                     } else {
-                        box[c] = eik2_newton(box[c], ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z);
+                        const unsigned m = fwd_orders2(dbits(old), dbits(box[c - 1]), dbits(box[c + 1]),
+                                                       dbits(box[c - R2]), dbits(box[c + R2]));
+                        sel |= m;
+                        if (m & obit) nv = eik2_newton(old, ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z);
+                    }
+                    if (!bits_same(old, nv)) {
+                        box[c] = nv;
+                        chg = true;
+                        if (lj == 0) chg_jlo = true;
+                        if (lj == ej - 1) chg_jhi = true;
                     }
                 }
             } else {
                 const unsigned fb = lj < 32 ? (fixed_lo >> lj) : (fixed_hi >> (lj - 32));
                 if (row_interior && gj >= 1 && gj <= nc - 2 && !(fb & 1u)) {
-                    Real r;
+                    const Real old = box[c];
+                    Real r = old;
                     if constexpr (KIND == kAdjPlain64) {
                         r = adj2_plain(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
                                        box[c - 1], box[c + R2], box[c - R2], A.dx, A.dz);
@@ -261,29 +325,55 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         r = adj2_bulk(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
                                       box[c - 1], box[c + R2], box[c - R2], (float)A.inv2x, (float)A.inv2z);
                     } else {
-                        r = adj2_polish(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
-                                        box[c - 1], box[c + R2], box[c - R2], box[c], A.inv2x, A.inv2z);
+                        const unsigned m = adj_orders2(dbits(tbox[c]), dbits(tbox[c - 1]), dbits(tbox[c + 1]),
+                                                       dbits(tbox[c - R2]), dbits(tbox[c + R2]));
+                        sel |= m;
+                        if (m & obit)
+                            r = adj2_polish(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
+                                            box[c - 1], box[c + R2], box[c - R2], old, A.inv2x, A.inv2z);
                     }
-                    box[c] = r;
+                    if (!bits_same(old, r)) {
+                        box[c] = r;
+                        chg = true;
+                        if (lj == 0) chg_jlo = true;
+                        if (lj == ej - 1) chg_jhi = true;
+                    }
                 }
             }
         }
         __syncwarp();
     }
 
-    bool changed = false;
+    if constexpr (kSelective) {
+        const unsigned tsel = __reduce_or_sync(0xffffffffu, sel);
+        if (lane == 0) dirty[tid] = (dirty[tid] & 0xf) | (int)(tsel << 4);
+    }
+    // nothing changed: field and snapshot comparison stand as they are
+    if (!__any_sync(0xffffffffu, chg)) return;
+    // unlock this tile and the face neighbours that see a changed face node (lane = row)
+    const unsigned f_ilo = __ballot_sync(0xffffffffu, chg && li == 0);
+    const unsigned f_ihi = __ballot_sync(0xffffffffu, chg && li == ei - 1);
+    const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
+    const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
+    if (lane == 0) {
+        dirty[tid] |= 0xf;
+        if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xf);
+        if (f_ihi && ti < A.nbi - 1) atomicOr(dirty + tid + A.nbj, 0xf);
+        if (f_jlo && tj > 0) atomicOr(dirty + tid - 1, 0xf);
+        if (f_jhi && tj < A.nbj - 1) atomicOr(dirty + tid + 1, 0xf);
+    }
+    bool moved = false;
     for (int y = 0; y < ei; ++y) {
         for (int x = lane; x < ej; x += 32) {
             const long long at = (long long)(i0 + y) * nc + j0 + x;
             const Real v = box[(y + 1) * R2 + x + 1];
             fld[at] = v;
-            if (A.last) {
-                const double diff = fabs((double)snp[at] - (double)v);
-                if (diff > A.tol_abs + A.tol_rel * fabs((double)v)) changed = true;
-            }
+            const double diff = fabs((double)__ldcg(snp + at) - (double)v);
+            if (diff > A.tol_abs + A.tol_rel * fabs((double)v)) moved = true;
         }
     }
-    if (A.last && __any_sync(0xffffffffu, changed) && lane == 0) A.changed[q] = 1;
+    const bool any_moved = __any_sync(0xffffffffu, moved);
+    if (lane == 0) A.diff[(long long)q * A.ntiles + tid] = any_moved ? 1 : 0;
 }
 
 template <int KIND>

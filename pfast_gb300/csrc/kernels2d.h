@@ -31,8 +31,14 @@ struct Sweep2Args {
     int nr, nc, nbi, nbj;
     double dx, dz;
     double inv2x, inv2z;         // (1.0/dx)/dx, (1.0/dz)/dz
+    float dxf, dzf;              // FP32 copies of dx, dz (no FP64 instruction in the FP32 sweeps)
     int dir;                     // 0..3: bit1 = s1>0 (rows), bit0 = s2>0 (cols); reference order
-    int first, last;
+    int iter;                    // outer iteration (snapshot stamps)
+    int ntiles;                  // tiles per instance (nbi * nbj)
+    int* dirty;                  // per (instance, tile): orders still due (bits 0-3), polish selection (4-7)
+    int* stamp;                  // per (instance, tile): iteration of the tile's snapshot
+    int* diff;                   // per (instance, tile): moved beyond the tolerance this iteration
+    unsigned long long* work;    // per instance: nodes of the tiles processed; may be null
     double tol_abs, tol_rel;
 };
 
