@@ -288,10 +288,23 @@ def main():
     dom = max(phases, key=lambda k: phases[k][0])
     ms_dom, upd_dom, w, kname = phases[dom]
     alg_bytes = upd_dom * 3 * w                       # read U + read slowness/T + write U per node update
+    # launches of that kernel per evaluation: outer iterations x 8 sweep orders x tile diagonals
+    # (4 x 8 x 32 tiles: nbk + nbi + nbj - 2 diagonals)
+    ndiag = -(-NZ // 4) + -(-NR // 8) + -(-NC // 32) - 2
+    iters_dom = {"fwd32": st["fwd32_iters_max"], "fwd64": st["fwd_iters_max"], "adj32": st["adj32_iters_max"],
+                 "adj64": st["adj_iters_max"]}[dom]
+    launches_dom = iters_dom * 8 * ndiag
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (ms_dom / 1e3) / 1e9 if ms_dom > 0 else 0.0
+    # DRAM bytes per launch of the polish kernels, measured with ncu (dram__bytes_read.sum +
+    # dram__bytes_write.sum over the 1680 launches of one evaluation on the 9-source case of this
+    # grid), per source of a launch; a launch's traffic grows with the sources it carries.
+    traffic_per_src = {"fwd64": 0.404e6, "adj64": 0.461e6}
+    traffic = traffic_per_src[dom] * len(srnum) if dom in traffic_per_src else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": kname, "phase": dom,
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_unit": "bytes per launch",
+                "algorithmic_bytes_per_launch": alg_bytes / launches_dom if launches_dom else None,
+                "kernel": kname, "phase": dom,
                 "peak_kind": peak_kind, "node_updates_per_s": upd_dom / (ms_dom / 1e3) if ms_dom > 0 else 0.0,
                 "phase_ms": ms_dom}
 
