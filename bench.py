@@ -214,6 +214,8 @@ def main():
     d_vp = torch.from_numpy(v0).cuda()
     grad = torch.empty_like(d_vp)
 
+    # ---- schedule autotuning on this workload (both schedules once, same bits), then warm-up
+    tune = sv.autotune(d_vp, precision=pg.PFAST_MIXED)
     # ---- device-resident timing (inputs already in HBM)
     for _ in range(args.warmup):
         sv.eval(d_vp, grad=grad, precision=pg.PFAST_MIXED)
@@ -338,6 +340,7 @@ def main():
                 "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                                "of": "one 256-source misfit+gradient evaluation, device-resident"},
                 "misfit": misfit,
+                "autotune_ms": {k: v["ms_total"] for k, v in tune.items()},
                 "step_ms": step_ms,
                 "phase_ms": {k: st[k] for k in ("ms_fwd32", "ms_fwd64", "ms_adj32", "ms_adj64", "ms_other", "ms_total")},
                 "iters": {k: st[k] for k in ("fwd32_iters_max", "fwd_iters_max", "adj32_iters_max", "adj_iters_max")}}

@@ -50,9 +50,11 @@ typedef struct {
                              (adjoint: times 1 + |lambda|) are dropped, so converged regions reach
                              a bitwise fixed point; 0 = the default, 1e-10.  Keep it well below the
                              1e-9 convergence tolerance. */
-    int schedule;         /* 3D sweeps: 0 = automatic, 1 = one launch per tile diagonal (every tile of
-                             every source spread over all SMs), 2 = persistent (one block solves one
-                             source; automatic picks it from 4 sources per SM).  Same results. */
+    int schedule;         /* 3D sweeps: 0 = automatic (the faster one measured by pfast_survey3d_autotune
+                             for this grid shape and source count; untuned: persistent from 4 sources
+                             per SM), 1 = one launch per tile diagonal (every tile of every source
+                             spread over all SMs), 2 = persistent (one block solves one source).
+                             Same results. */
     int near_source_radius;  /* 3D forward, opt-in (not in the reference): nodes within this many grid
                              nodes of the source (Euclidean, in nodes) start from the straight-ray
                              traveltime 0.5*(s_src + s_node)*distance and stay fixed, which removes most
@@ -137,6 +139,13 @@ pfast_status pfast_survey3d_eval(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
 /* First-arrival picks (T_PFAST3D.cpp:672-686).  vp, picks: DEVICE arrays; picks[nrec]. */
 pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp,
                                     const pfast_options* opt, double* picks, pfast_stats* stats);
+
+/* Schedule autotuner: runs the survey's evaluation (gradient when it has picks, else picks)
+ * once per sweep schedule on the DEVICE model vp and records each phase's time per (sweep
+ * kind, grid shape, source count); later automatic-schedule calls of the same shape use the
+ * faster schedule.  Both schedules give identical results.  stats_*: optional. */
+pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
+                                     pfast_stats* stats_diagonal, pfast_stats* stats_persistent);
 
 /* One-call host-buffer forms (copies in and out inside the call). */
 pfast_status pfast_eval3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy,

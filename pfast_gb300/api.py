@@ -183,6 +183,16 @@ class Survey3D:
                                         _dev_ptr(grad, "grad", numel=n), C.addressof(E), C.byref(st)), "survey3d_eval")
         return grad, E.value, st.as_dict()
 
+    def autotune(self, vp, precision=PFAST_MIXED, maxswp=100):
+        """Time both sweep schedules on this survey and model (pfast_survey3d_autotune); later
+        automatic-schedule evaluations of this grid and source count use the faster one.
+        Returns the per-schedule stats."""
+        sd, sp = _capi.Stats(), _capi.Stats()
+        o = _opts(precision, maxswp, 0)
+        check(lib().pfast_survey3d_autotune(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=int(np.prod(self.shape))),
+                                            C.byref(o), C.byref(sd), C.byref(sp)), "survey3d_autotune")
+        return {"diagonal": sd.as_dict(), "persistent": sp.as_dict()}
+
     def forward(self, vp, picks=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0, polish_floor=0.0,
                 schedule=0, near_source_radius=0):
         """First-arrival picks [sum(srnum)] for the device model vp.  Returns (picks, stats)."""

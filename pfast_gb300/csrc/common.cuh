@@ -34,7 +34,6 @@ constexpr int SJ = TJ + 2, SPS = 297;
 static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
 // Warps (tiles) per CTA.
 constexpr int kMaxPWarps = 16;   // warps per block of the persistent sweep kernel, at most
-constexpr int kPersistentPerSM = 4;   // instances per SM from which the persistent schedule is used
 constexpr int kWarps3 = 1;   // one-warp CTAs: the finest shared-memory granularity, hence the most warps per SM
 
 // ---------------------------------------------------------------- 2D tiles

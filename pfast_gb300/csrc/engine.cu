@@ -156,6 +156,34 @@ Spacing3 make_spacing(double dx, double dy, double dz) {
 
 // Run outer iterations of `kind` over the active batch instances until each one
 // converges or reaches maxiter.  iters[b] receives the iteration count of instance b.
+// Schedule autotuner, per (device, sweep kind, grid, active instances): phase times of the two
+// schedules measured by pfast_survey3d_autotune, which runs the same evaluation once with each
+// (identical inputs, identical bits).  An automatic phase uses the faster one once both are
+// known; before that, the persistent kernel from 4 instances per SM, else one launch per tile
+// diagonal.
+struct TuneEntry {
+    double ms[2] = {0.0, 0.0};
+    int n[2] = {0, 0};
+};
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int, int, int>, TuneEntry> g_tune;
+
+static int tuned_schedule(const std::tuple<int, int, int, int, int, int>& key, int sms) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end() && it->second.n[0] > 0 && it->second.n[1] > 0)
+        return it->second.ms[1] / it->second.n[1] < it->second.ms[0] / it->second.n[0] ? 1 : 0;
+    return std::get<5>(key) >= 4 * sms ? 1 : 0;
+}
+
+static void tune_record(const std::tuple<int, int, int, int, int, int>& key, int which, double ms) {
+    if (!(ms > 0.0)) return;
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    TuneEntry& e = g_tune[key];
+    e.ms[which] += ms;
+    e.n[which] += 1;
+}
+
 pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable3& dt, int nb,
                          std::vector<int>& active, int maxiter, int* iters, long long nodes_per_sweep,
                          long long* node_updates, int* not_conv, double* ms_acc) {
@@ -197,12 +225,14 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     // Two schedules.  Per-diagonal launches spread every tile of every active instance over
     // all SMs (one warp per tile) and suit surveys with few instances per SM, such as 256
     // sources on 152 SMs; the persistent kernel (one block solves one instance, no host
-    // round trip per iteration) suits runs with several instances per SM.
+    // round trip per iteration) suits runs with several instances per SM.  Automatic: the
+    // autotuner above.
     int dev = 0, sms = 1;
     PFAST_CUDA_TRY(cudaGetDevice(&dev));
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const auto tkey = std::make_tuple(dev, kind, a.nz, a.nr, a.nc, (int)active.size());
     const bool persistent = ctx->schedule == PFAST_SCHEDULE_PERSISTENT ||
-                            (ctx->schedule == PFAST_SCHEDULE_AUTO && (int)active.size() >= kPersistentPerSM * sms);
+                            (ctx->schedule == PFAST_SCHEDULE_AUTO && !active.empty() && tuned_schedule(tkey, sms) == 1);
     if (persistent && maxiter > 0) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
@@ -253,13 +283,16 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     }
     if (not_conv) *not_conv += (int)active.size();
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[1], st));
-    if (node_updates) {
-        unsigned long long* hw = ctx->h_work.as<unsigned long long>();
-        PFAST_CUDA_TRY(cudaMemcpyAsync(hw, a.work, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, st));
-        PFAST_CUDA_TRY(cudaStreamSynchronize(st));
-        for (int b = 0; b < nb; ++b) *node_updates += (long long)hw[b];
-    }
-    add_elapsed(ctx->ev[0], ctx->ev[1], ms_acc);
+    unsigned long long* hw = ctx->h_work.as<unsigned long long>();
+    PFAST_CUDA_TRY(cudaMemcpyAsync(hw, a.work, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, st));
+    PFAST_CUDA_TRY(cudaStreamSynchronize(st));
+    long long upd = 0;
+    for (int b = 0; b < nb; ++b) upd += (long long)hw[b];
+    if (node_updates) *node_updates += upd;
+    double ms = 0.0;
+    add_elapsed(ctx->ev[0], ctx->ev[1], &ms);
+    if (ms_acc) *ms_acc += ms;
+    if (ctx->tuning) tune_record(tkey, persistent ? 1 : 0, ms);
     return PFAST_OK;
 }
 
@@ -771,6 +804,26 @@ pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const do
                                     double* picks, pfast_stats* stats) {
     if (!picks) { set_last_error("null picks"); return PFAST_ERR_INVALID; }
     return survey3d_run(ctx, sv, vp, opt, nullptr, nullptr, picks, stats);
+}
+
+pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
+                                     pfast_stats* stats_diagonal, pfast_stats* stats_persistent) {
+    if (!ctx || !sv || !vp) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
+    if (!valid_options(opt)) return PFAST_ERR_INVALID;
+    const long long N = (long long)sv->nz * sv->nr * sv->nc;
+    PFAST_TRY(ctx->out_a.ensure(sizeof(double) * std::max<long long>(N, sv->nrec)));
+    pfast_options o = resolve(opt, 100);
+    pfast_stats* sts[2] = {stats_diagonal, stats_persistent};
+    ctx->tuning = true;
+    pfast_status r = PFAST_OK;
+    for (int which = 0; which < 2 && r == PFAST_OK; ++which) {
+        o.schedule = which == 0 ? PFAST_SCHEDULE_DIAGONAL : PFAST_SCHEDULE_PERSISTENT;
+        double E = 0.0;
+        r = sv->has_picks ? survey3d_run(ctx, sv, vp, &o, ctx->out_a.as<double>(), &E, nullptr, sts[which])
+                          : survey3d_run(ctx, sv, vp, &o, nullptr, nullptr, ctx->out_a.as<double>(), sts[which]);
+    }
+    ctx->tuning = false;
+    return r;
 }
 
 pfast_status pfast_eval3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy, double dz,

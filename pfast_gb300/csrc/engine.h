@@ -59,6 +59,7 @@ struct pfast_ctx {
     float polish_floor = pfast::kPolishFloor;   // of the current 3D evaluation (pfast_options)
     int schedule = PFAST_SCHEDULE_AUTO;         // of the current 3D evaluation (pfast_options)
     int near_radius = 0;                        // of the current 3D evaluation (pfast_options)
+    bool tuning = false;                        // record phase times for the schedule autotuner
 };
 
 struct pfast_survey3d {

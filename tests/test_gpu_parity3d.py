@@ -276,3 +276,21 @@ def test_near_source_initialisation_reduces_the_source_error(ctx):
     p1, _ = sv.forward(d_vp, precision=pg.PFAST_PLAIN_FP64, near_source_radius=0)
     assert bits_equal(p0.cpu().numpy(), p1.cpu().numpy())
     sv.close()
+
+
+def test_schedule_autotune(ctx):
+    """pfast_survey3d_autotune times both sweep schedules on the same evaluation; automatic
+    evaluations afterwards use the faster one and give the same bits as either forced one."""
+    import torch
+    pg = _pg()
+    h = (10.0, 10.0, 10.0)
+    vp, src, srnum, rec, nxyz, noise = case3d((12, 16, 20), h, 41)
+    tobs = 0.2 + noise
+    sv = pg.Survey3D(ctx, 16, 20, 12, *h, src, srnum, rec, nxyz, tobs)
+    d_vp = torch.from_numpy(vp).cuda()
+    t = sv.autotune(d_vp, precision=pg.PFAST_MIXED)
+    assert t["diagonal"]["ms_total"] > 0 and t["persistent"]["ms_total"] > 0
+    g_auto, e_auto, _ = sv.eval(d_vp, precision=pg.PFAST_MIXED)
+    g_diag, e_diag, _ = sv.eval(d_vp, precision=pg.PFAST_MIXED, schedule=pg._capi.PFAST_SCHEDULE_DIAGONAL)
+    assert bits_equal(g_auto.cpu().numpy(), g_diag.cpu().numpy()) and e_auto == e_diag
+    sv.close()
