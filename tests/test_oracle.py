@@ -19,6 +19,13 @@ from oracle import port, ref
 from helpers import GOLDEN, bits_equal, case3d, load_fw, load_inv, picks_from
 
 
+@pytest.fixture(autouse=True)
+def _in_tmp_cwd(tmp_path, monkeypatch):
+    """The reference's code writes a debug dump into the working directory when an adjoint
+    solve reaches its iteration cap; keep it out of the checkout."""
+    monkeypatch.chdir(tmp_path)
+
+
 def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
