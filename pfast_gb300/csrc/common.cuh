@@ -68,6 +68,26 @@ __device__ __forceinline__ double min_nonneg(double x, double y) { return dbits(
 __device__ __forceinline__ double pos_sign(double e) { return __double2hiint(e) < 0 ? 0.0 : e; }
 __device__ __forceinline__ double neg_sign(double e) { return __double2hiint(e) < 0 ? e : 0.0; }
 
+// FP64 <-> FP32 conversions on the integer pipe, from the IEEE 754 binary64/binary32
+// layouts (sign | exponent | fraction; biases 1023 and 127).  narrow_trunc keeps the top
+// 23 fraction bits (truncation); magnitudes below 2^-126 give 0 and above 2^127 give
+// +-FLT_MAX.  widen_exact is exact for normal floats and maps zero and subnormals to 0.
+// They serve the polish updates, whose step sizes and derivative scales need FP32
+// precision only.
+__device__ __forceinline__ float narrow_trunc(double x) {
+    const long long b = dbits(x);
+    const unsigned hi = (unsigned)((unsigned long long)b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u, mag = hi & 0x7fffffffu;
+    if (mag < (897u << 20)) return 0.0f;
+    if (mag >= (1151u << 20)) return __uint_as_float(sign | 0x7f7fffffu);
+    return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ double widen_exact(float f) {
+    const unsigned u = __float_as_uint(f), mag = u & 0x7fffffffu;
+    if (mag < 0x00800000u) return 0.0;
+    return __hiloint2double((int)((u & 0x80000000u) | ((mag >> 3) + (896u << 20))), (int)(mag << 29));
+}
+
 // Which kernel flavour a sweep runs.
 enum SweepKind : int {
     kFwdPlain64 = 0,   // reference arithmetic, FP64, U = min(U, q)

@@ -36,14 +36,22 @@ template <> struct Traits<kAdjPlain64>   { using Real = double; using Aux = doub
 template <> struct Traits<kAdjFast32>    { using Real = float;  using Aux = float;  static constexpr bool adj = true; };
 template <> struct Traits<kAdjPolish64>  { using Real = double; using Aux = double; static constexpr bool adj = true; };
 
-// Shared memory per warp: the field's halo box, plus the traveltime halo box for
-// the adjoint.  The forward's slowness is read per node through L1 (each lane walks
-// its own row, so a fetched line serves the next steps): keeping it out of shared
-// memory raises the number of resident warps.
+// Whether the adjoint's traveltime is read through register windows and warp shuffles
+// (FP64 kinds, whose two FP64 boxes would halve the resident warps) or staged as a halo
+// box like the field (FP32 bulk: a small box, and a coalesced load beats per-lane reads).
+template <int KIND>
+__host__ __device__ constexpr bool t_windows() {
+    return Traits<KIND>::adj && sizeof(typename Traits<KIND>::Aux) == 8;
+}
+
+// Shared memory per warp: the field's halo box, plus the FP32 bulk adjoint's traveltime
+// box.  The forward's slowness is read per node through L1 (each lane walks its own row,
+// so a fetched line serves the next steps).
 template <int KIND>
 __host__ __device__ constexpr int warp_smem_bytes() {
     using T = Traits<KIND>;
-    return int(HK * PS * sizeof(typename T::Real) + (T::adj ? HK * PS * sizeof(typename T::Aux) : 0));
+    return int(HK * PS * sizeof(typename T::Real) +
+               (T::adj && !t_windows<KIND>() ? HK * PS * sizeof(typename T::Aux) : 0));
 }
 
 __device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
@@ -111,28 +119,30 @@ __device__ __forceinline__ float eik3_fast(float a, float b, float c, float s, c
 // src/T_pfsm3d.h:106-118 are the pieces of f).  f in FP64, the step f/f' in FP32.
 // s2 = s^2 (precomputed); the rare restart branch (U0 at or below every
 // neighbour) takes the 1-term value with the slowness itself.
+// big: the step leaves a second-order remainder (about sum_active(w) step^2 / f') above the
+// floor, so the node wants another Newton step in the same order.
 __device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s2, const double* slow,
-                                              long long node, const Spacing3& sp, float floor) {
+                                              long long node, const Spacing3& sp, float floor, bool& big) {
+    // FP64 for what fixes the root (the differences and the residual f, 8 FP64 instructions
+    // in the isotropic case); the derivative f' and the step in FP32.
     const double px = pos_sign(U0 - a), py = pos_sign(U0 - b), pz = pos_sign(U0 - c);
-    double f, g;
-    if (sp.iso) {
-        f = fma(sp.inv2[0], fma(px, px, fma(py, py, pz * pz)), -s2);
-        g = (px + py) + pz;
-    } else {
-        f = fma(sp.inv2[0] * px, px, fma(sp.inv2[1] * py, py, fma(sp.inv2[2] * pz, pz, -s2)));
-        g = 0.0;
-    }
-    float fp;
-    if (sp.iso) fp = 2.0f * sp.wf[0] * (float)g;
-    else fp = 2.0f * (sp.wf[0] * (float)px + sp.wf[1] * (float)py + sp.wf[2] * (float)pz);
+    double f;
+    if (sp.iso) f = fma(sp.inv2[0], fma(px, px, fma(py, py, pz * pz)), -s2);
+    else f = fma(sp.inv2[0] * px, px, fma(sp.inv2[1] * py, py, fma(sp.inv2[2] * pz, pz, -s2)));
+    const float fx = narrow_trunc(px), fy = narrow_trunc(py), fz = narrow_trunc(pz);
+    const float fp = 2.0f * (sp.wf[0] * fx + sp.wf[1] * fy + sp.wf[2] * fz);
     if (!(fp > 0.0f)) {
+        big = true;
         const double s = __ldg(slow + node);
         return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
     }
-    const float step = __fdividef((float)f, fp);
+    const float step = __fdividef(narrow_trunc(f), fp);
+    const float sw = (dbits(px) > 0 ? sp.wf[0] : 0.0f) + (dbits(py) > 0 ? sp.wf[1] : 0.0f) +
+                     (dbits(pz) > 0 ? sp.wf[2] : 0.0f);   // p >= 0: integer tests keep the FP64 pipe free
+    big = sw * step * step > floor * fp;
     // corrections far below the 1e-9 convergence tolerance are dropped, so that a
     // converged region reaches a bitwise fixed point (and its tiles lock)
-    return fabsf(step) <= floor ? U0 : U0 - (double)step;
+    return fabsf(step) <= floor ? U0 : U0 - widen_exact(step);
 }
 
 // Adjoint updates.  The reference's upwind formula (src/T_padjoint3d.h:51-66)
@@ -189,31 +199,38 @@ __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float
     return fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r;
 }
 
-// FP64 polish adjoint update in residual-correction form: num, den and the residual
-// r = num - den*lambda0 in FP64 (max(+-e, 0) by the sign bit), the step r/den in FP32.
+// FP64 polish adjoint update in residual-correction form.  With mu_m = lambda_m where
+// e_m > 0 and lambda0 where e_m < 0, the residual is
+//   r = num - den*lambda0 = sum_m w_m e_m mu_m,
+// formed in FP64 (the differences e_m are exact, Sterbenz); den = -sum_m w_m min(e_m, 0)
+// only scales the step r/den and is formed in FP32, as is the step.  The fixed point is
+// r = 0 in FP64.  13 FP64 instructions in the isotropic case.
 __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm, double Typ, double Tym, double Tzp,
                                               double Tzm, double Lxp, double Lxm, double Lyp, double Lym, double Lzp,
-                                              double Lzm, double L0, const Spacing3& sp, float floor) {
+                                              double Lzm, double L0, const Spacing3& sp, float floor, bool& big) {
     if (unreached64(T0, Txp, Txm, Typ, Tym, Tzp, Tzm)) return 0.0;
     const double exp_ = Txp - T0, exm = Txm - T0, eyp = Typ - T0, eym = Tym - T0, ezp = Tzp - T0, ezm = Tzm - T0;
-    double num, den;   // den is accumulated with the sign flipped: -sum w min(e, 0)
+    auto mu = [&](double e, double L) { return __double2hiint(e) < 0 ? L0 : L; };
+    auto nf = [](double e) { return __double2hiint(e) < 0 ? -narrow_trunc(e) : 0.0f; };   // max(-e, 0)
+    double r;
+    float den;
     if (sp.iso) {
-        den = ((neg_sign(exp_) + neg_sign(exm)) + (neg_sign(eyp) + neg_sign(eym))) + (neg_sign(ezp) + neg_sign(ezm));
-        num = fma(pos_sign(exp_), Lxp, fma(pos_sign(exm), Lxm, fma(pos_sign(eyp), Lyp,
-              fma(pos_sign(eym), Lym, fma(pos_sign(ezp), Lzp, pos_sign(ezm) * Lzm)))));
-        den = -sp.inv2[0] * den;
-        num = sp.inv2[0] * num;
+        r = fma(exp_, mu(exp_, Lxp), fma(exm, mu(exm, Lxm), fma(eyp, mu(eyp, Lyp),
+            fma(eym, mu(eym, Lym), fma(ezp, mu(ezp, Lzp), ezm * mu(ezm, Lzm))))));
+        den = ((nf(exp_) + nf(exm)) + (nf(eyp) + nf(eym))) + (nf(ezp) + nf(ezm));
+        if (!(den * sp.wf[0] > 1e-9f)) return 0.0;
     } else {
-        const double wx = sp.inv2[0], wy = sp.inv2[1], wz = sp.inv2[2];
-        den = -(wx * (neg_sign(exp_) + neg_sign(exm)) + wy * (neg_sign(eyp) + neg_sign(eym)) +
-                wz * (neg_sign(ezp) + neg_sign(ezm)));
-        num = wx * fma(pos_sign(exp_), Lxp, pos_sign(exm) * Lxm) + wy * fma(pos_sign(eyp), Lyp, pos_sign(eym) * Lym) +
-              wz * fma(pos_sign(ezp), Lzp, pos_sign(ezm) * Lzm);
+        const double rx = fma(exp_, mu(exp_, Lxp), exm * mu(exm, Lxm));
+        const double ry = fma(eyp, mu(eyp, Lyp), eym * mu(eym, Lym));
+        const double rz = fma(ezp, mu(ezp, Lzp), ezm * mu(ezm, Lzm));
+        r = fma(sp.inv2[0], rx, fma(sp.inv2[1], ry, sp.inv2[2] * rz));
+        den = sp.wf[0] * (nf(exp_) + nf(exm)) + sp.wf[1] * (nf(eyp) + nf(eym)) + sp.wf[2] * (nf(ezp) + nf(ezm));
+        if (!(den > 1e-9f)) return 0.0;
     }
-    if (!(dbits(den) > dbits(1e-9))) return 0.0;   // den >= 0 by construction
-    const double r = fma(-den, L0, num);
-    const float step = __fdividef((float)r, (float)den);
-    return fabsf(step) <= floor * (1.0f + fabsf((float)L0)) ? L0 : L0 + (double)step;
+    const float step = __fdividef(narrow_trunc(r), den);
+    const float tol = floor * (1.0f + fabsf(narrow_trunc(L0)));
+    big = fabsf(step) * 1.2e-7f > tol;   // the local equation is linear: only the FP32 step's error remains
+    return fabsf(step) <= tol ? L0 : L0 + widen_exact(step);
 }
 
 // ----------------------------------------------------------- tile I/O
@@ -290,6 +307,11 @@ __device__ __forceinline__ unsigned adj_orders(long long t, long long xlo, long 
     return m;
 }
 
+// ----------------------------------------------------------- dependency-aware marking
+// Ordered integer of a value >= 0 (its bit pattern), for FP32 and FP64 fields.
+__device__ __forceinline__ long long obits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ long long obits(float x) { return __float_as_int(x); }
+
 // ----------------------------------------------------------- the sweep kernel
 // Tile locking: a tile whose processing changed no bit of its field, and none of
 // whose face neighbours has changed a face node since, is a fixed point of the node
@@ -355,6 +377,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
     Real* box = reinterpret_cast<Real*>(wsm);
     Aux* aux = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
+    constexpr bool TWIN = t_windows<KIND>();
     Real* fld = reinterpret_cast<Real*>(A.field) + inst * A.fstride;
     Real* snp = reinterpret_cast<Real*>(A.snap) + inst * A.fstride;
 
@@ -370,8 +393,9 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     const int lk = pz ? lkf : ek - 1 - lkf;
     const int li = py ? lif : ei - 1 - lif;
     if constexpr (ADJ) {
-        const Aux* T = reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride;
-        load_box<Aux, false>(aux, T, k0, i0, j0, nz, nr, nc, Aux(0), lane);
+        if constexpr (!TWIN)
+            load_box<Aux, false>(aux, reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride, k0, i0, j0, nz, nr, nc,
+                                 Aux(0), lane);
         if (lane_ok)
             fixed_bits = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
     }
@@ -401,16 +425,87 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     unsigned sel = 0;   // polish: orders in which some node of this lane's pencil is selected
     const long long rowbase = gk * plane + (long long)gi * nc;
     bool chg = false, chg_jlo = false, chg_jhi = false;   // this lane's pencil changed (anywhere / at lj = 0 / at ej-1)
+    // Face marks: a changed face node that a node of the face neighbour depends on.  The
+    // plain kinds mark every changed face node (their tile skipping must stay exact).
+    // Elsewhere the dependency is one-directional: a forward update reads only neighbours
+    // below the node's value (the Godunov update and its Newton form exclude larger ones),
+    // and lambda at a node reads only neighbours of larger traveltime.
+    constexpr bool kPrune = KIND != kFwdPlain64 && KIND != kAdjPlain64;
+    bool m_klo = false, m_khi = false, m_ilo = false, m_ihi = false;
+    bool restep = false;   // polish: some update left a remainder above the floor (visit again in this order)
+
+    // ---- adjoint traveltime windows (FP64 kinds).  Lane (kf, if) (flipped coordinates) is at flipped
+    // position jf = t - kf - if in step t and keeps its pencil's traveltimes at jf-1, jf, jf+1
+    // (tm, t0, tp), with loads issued three steps ahead (q1, q2).  Lane (kf-1, if) is one
+    // position ahead, so its tm is the traveltime at (kf-1, if, jf); lane (kf+1, if) is one
+    // behind and its tp is the one at (kf+1, if, jf); likewise along if.  The halo pencils
+    // outside the tile are tracked by owner lanes 0-23 at their consumer's position:
+    // lanes 0-7 the flipped k-1 face, 8-15 the k+1 face, 16-19 the i-1 face, 20-23 the i+1 face.
+    const Aux* Tb = TWIN ? reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride : nullptr;
+    const Aux* trow = (TWIN && lane_ok) ? Tb + rowbase : nullptr;
+    const Aux* hrow = nullptr;
+    int hpos = 0;
+    if constexpr (TWIN) {
+        int lkh = 0, lih = 0;
+        bool own = false;
+        if (lane < 8) {
+            own = lane < ei; lkh = pz ? -1 : ek; lih = py ? lane : ei - 1 - lane; hpos = lane;
+        } else if (lane < 16) {
+            const int x = lane - 8;
+            own = x < ei; lkh = pz ? ek : -1; lih = py ? x : ei - 1 - x; hpos = ek - 1 + x;
+        } else if (lane < 24) {
+            const int y = (lane - 16) & 3;
+            const bool lo = lane < 20;
+            own = y < ek; lkh = pz ? y : ek - 1 - y;
+            lih = lo ? (py ? -1 : ei) : (py ? ei : -1);
+            hpos = lo ? y : y + ei - 1;
+        }
+        const int gkh = k0 + lkh, gih = i0 + lih;
+        if (own && (unsigned)gkh < (unsigned)nz && (unsigned)gih < (unsigned)nr) hrow = Tb + gkh * plane + (long long)gih * nc;
+    }
+    // traveltime of pencil row r at flipped position p, zero outside [plo, phi] or the grid
+    auto tload = [&](const Aux* r, int p, int plo, int phi) -> Aux {
+        const int g = j0 + (px ? p : ej - 1 - p);
+        return (r != nullptr && p >= plo && p <= phi && (unsigned)g < (unsigned)nc) ? __ldg(r + g) : Aux(0);
+    };
+    const int jf0 = -lkf - lif;
+    Aux tm = Aux(0), t0 = Aux(0), tp = Aux(0), q1 = Aux(0), q2 = Aux(0), h0 = Aux(0), hq1 = Aux(0), hq2 = Aux(0);
+    if constexpr (TWIN) {
+        tm = tload(trow, jf0 - 1, -1, ej); t0 = tload(trow, jf0, -1, ej); tp = tload(trow, jf0 + 1, -1, ej);
+        q1 = tload(trow, jf0 + 2, -1, ej); q2 = tload(trow, jf0 + 3, -1, ej);
+        h0 = tload(hrow, -hpos, 0, ej - 1); hq1 = tload(hrow, 1 - hpos, 0, ej - 1); hq2 = tload(hrow, 2 - hpos, 0, ej - 1);
+    }
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
         const int ljf = t - lkf - lif;
+        // adjoint: the traveltimes around this lane's node, in grid orientation
+        Aux Txm = Aux(0), Txp = Aux(0), Tym = Aux(0), Typ = Aux(0), Tzm = Aux(0), Tzp = Aux(0);
+        if constexpr (TWIN) {
+            const Aux a = __shfl_sync(0xffffffffu, tm, (lane - TI) & 31);
+            const Aux b = __shfl_sync(0xffffffffu, tp, (lane + TI) & 31);
+            const Aux c_ = __shfl_sync(0xffffffffu, tm, (lane - 1) & 31);
+            const Aux d = __shfl_sync(0xffffffffu, tp, (lane + 1) & 31);
+            const Aux hkl = __shfl_sync(0xffffffffu, h0, lif);
+            const Aux hkh = __shfl_sync(0xffffffffu, h0, 8 + lif);
+            const Aux hil = __shfl_sync(0xffffffffu, h0, 16 + (lkf & 3));
+            const Aux hih = __shfl_sync(0xffffffffu, h0, 20 + (lkf & 3));
+            const Aux zkm = lkf == 0 ? hkl : a, zkp = lkf == ek - 1 ? hkh : b;
+            const Aux yim = lif == 0 ? hil : c_, yip = lif == ei - 1 ? hih : d;
+            Tzm = pz ? zkm : zkp; Tzp = pz ? zkp : zkm;
+            Tym = py ? yim : yip; Typ = py ? yip : yim;
+            Txm = px ? tm : tp;   Txp = px ? tp : tm;
+        }
         if (lane_ok && ljf >= 0 && ljf < ej) {
             const int lj = px ? ljf : ej - 1 - ljf;
             const int c = cbase + lj;
             const int gj = j0 + lj;
             const Real old = box[c];
             Real nv = old;
+            if constexpr (ADJ && !TWIN) {   // FP32 bulk: the traveltimes from the staged box
+                t0 = aux[c]; Txm = aux[c - 1]; Txp = aux[c + 1]; Tym = aux[c - HJ]; Typ = aux[c + HJ];
+                Tzm = aux[c - PS]; Tzp = aux[c + PS];
+            }
             if constexpr (!ADJ) {
                 const int qk = gk - sk, qi = gi - si, qj = gj - sj;
                 if (qk * qk + qi * qi + qj * qj > A.src_r2) {   // the source node (and the opt-in fixed region) stays
@@ -440,33 +535,34 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                             const double xa = min_nonneg(box[c + 1], box[c - 1]);
                             const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
                             const double zc = min_nonneg(box[c - PS], box[c + PS]);
-                            nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp, A.polish_floor);
+                            bool big = false;
+                            nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp, A.polish_floor, big);
+                            restep |= big;
                         }
                     }
                 }
             } else {
                 if (row_interior && gj >= 1 && gj <= nc - 2 && !((fixed_bits >> lj) & 1u)) {
                     if constexpr (KIND == kAdjPlain64) {
-                        nv = adj3_plain(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                        aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                        box[c - PS], A.sp);
+                        nv = adj3_plain(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
+                                        box[c - HJ], box[c + PS], box[c - PS], A.sp);
                     } else if constexpr (KIND == kAdjFast32) {
-                        nv = adj3_bulk(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                       aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ], box[c + PS],
-                                       box[c - PS], old, A.sp);
+                        nv = adj3_bulk(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
+                                       box[c - HJ], box[c + PS], box[c - PS], old, A.sp);
                     } else {
                         // Octant selection (see the forward polish): lambda at a node depends on the
                         // neighbours with a larger traveltime.  Where on some axis only the neighbour
                         // visited after the node is larger, the node waits for its own sweep; where
                         // both are larger no sweep order has both fresh, and the node is updated.
-                        const unsigned m = adj_orders(dbits(aux[c]), dbits(aux[c - 1]), dbits(aux[c + 1]),
-                                                      dbits(aux[c - HJ]), dbits(aux[c + HJ]), dbits(aux[c - PS]),
-                                                      dbits(aux[c + PS]));
+                        const unsigned m = adj_orders(dbits(t0), dbits(Txm), dbits(Txp), dbits(Tym), dbits(Typ),
+                                                      dbits(Tzm), dbits(Tzp));
                         sel |= m;
-                        if (m & obit)
-                            nv = adj3_polish(aux[c], aux[c + 1], aux[c - 1], aux[c + HJ], aux[c - HJ], aux[c + PS],
-                                             aux[c - PS], box[c + 1], box[c - 1], box[c + HJ], box[c - HJ],
-                                             box[c + PS], box[c - PS], old, A.sp, A.polish_floor);
+                        if (m & obit) {
+                            bool big = false;
+                            nv = adj3_polish(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
+                                             box[c - HJ], box[c + PS], box[c - PS], old, A.sp, A.polish_floor, big);
+                            restep |= big;
+                        }
                     }
                 }
             }
@@ -476,9 +572,28 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             if (bo != bn) {
                 box[c] = nv;
                 chg = true;
-                if (lj == 0) chg_jlo = true;
-                if (lj == ej - 1) chg_jhi = true;
+                if constexpr (kPrune) {
+                    // the neighbour node across a face (box index n, traveltime tn): does it
+                    // depend on this node?
+                    auto dep = [&](int n, Aux tn) {
+                        if constexpr (ADJ) return obits(t0) > obits(tn);
+                        else return min(obits(old), obits(nv)) < obits(box[n]);
+                    };
+                    if (lk == 0 && dep(c - PS, Tzm)) m_klo = true;
+                    if (lk == ek - 1 && dep(c + PS, Tzp)) m_khi = true;
+                    if (li == 0 && dep(c - HJ, Tym)) m_ilo = true;
+                    if (li == ei - 1 && dep(c + HJ, Typ)) m_ihi = true;
+                    if (lj == 0 && dep(c - 1, Txm)) chg_jlo = true;
+                    if (lj == ej - 1 && dep(c + 1, Txp)) chg_jhi = true;
+                } else {
+                    if (lj == 0) chg_jlo = true;
+                    if (lj == ej - 1) chg_jhi = true;
+                }
             }
+        }
+        if constexpr (TWIN) {   // slide the windows to step t + 1
+            tm = t0; t0 = tp; tp = q1; q1 = q2; q2 = tload(trow, t + 4 - lkf - lif, -1, ej);
+            h0 = hq1; hq1 = hq2; hq2 = tload(hrow, t + 3 - hpos, 0, ej - 1);
         }
         __syncwarp();
     }
@@ -492,17 +607,21 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     if (!__any_sync(0xffffffffu, chg)) return;
 
     // ---- unlock this tile and every face neighbour that sees a changed face node
-    const unsigned f_klo = __ballot_sync(0xffffffffu, chg && lk == 0);
-    const unsigned f_khi = __ballot_sync(0xffffffffu, chg && lk == ek - 1);
-    const unsigned f_ilo = __ballot_sync(0xffffffffu, chg && li == 0);
-    const unsigned f_ihi = __ballot_sync(0xffffffffu, chg && li == ei - 1);
+    const unsigned f_klo = __ballot_sync(0xffffffffu, kPrune ? m_klo : chg && lk == 0);
+    const unsigned f_khi = __ballot_sync(0xffffffffu, kPrune ? m_khi : chg && lk == ek - 1);
+    const unsigned f_ilo = __ballot_sync(0xffffffffu, kPrune ? m_ilo : chg && li == 0);
+    const unsigned f_ihi = __ballot_sync(0xffffffffu, kPrune ? m_ihi : chg && li == ei - 1);
     const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
     const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
+    // A polish sweep in order o leaves every node that selects o consistent with the values
+    // it reads (its active neighbours come before it in o), so after small updates the tile
+    // is due again in o only when a neighbour or another order changes something.
+    const bool again = !kSelective || __any_sync(0xffffffffu, restep);
     if (lane == 0) {
         // neighbours keep their selection bits: OR in the eight order bits (two tiles of one
         // launch can share a face neighbour, hence atomic)
         const int sk_ = A.nbi * A.nbj;
-        dirty[tid] |= 0xff;
+        dirty[tid] |= again ? 0xff : (0xff & ~obit);
         if (f_klo && tk > 0) atomicOr(dirty + tid - sk_, 0xff);
         if (f_khi && tk < A.nbk - 1) atomicOr(dirty + tid + sk_, 0xff);
         if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xff);
