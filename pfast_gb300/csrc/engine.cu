@@ -779,7 +779,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
         if (want_grad) {
             PFAST_TRY(adjoint3d_batch(ctx, sv, b0, nb, o.precision, o.maxswp, ee.data(), stats));
             for (int b = 0; b < nb; ++b) E += ee[b];   // loc_E += EE in source order
-            PFAST_LAUNCH(ctx, launch_accumulate(grad, ctx->L64.as<double>(), N, vp, N, nb, s));
+            PFAST_LAUNCH(ctx, launch_accumulate(grad, ctx->L64.as<double>(), N, vp, N, nb, o.precision == PFAST_PLAIN_FP64, s));
         }
         if (picks) PFAST_LAUNCH(ctx, launch_gather3(ctx->T64.as<double>(), N, sv->d_rec, sv->d_ch0 + b0, sv->d_srnum + b0, nb,
                                             sv->nz, sv->nr, sv->nc, picks, s));

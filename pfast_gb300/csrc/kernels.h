@@ -108,7 +108,7 @@ pfast_status launch_bc3(const Bc3Args& a, int nbatch, cudaStream_t st);
 
 // grad[n] <- grad[n] - lam_b[n] / (v*v*v), b = 0..nbatch-1 in order (src/T_PFAST3D.cpp:393).
 pfast_status launch_accumulate(double* grad, const double* lam, long long fstride, const double* vp, long long n,
-                               int nbatch, cudaStream_t st);
+                               int nbatch, bool exact, cudaStream_t st);
 // picks[row] = T_b[rec[row]] for rows of each batch source.
 pfast_status launch_gather3(const double* T, long long fstride, const int* rec, const int* ch0, const int* srnum,
                             int nbatch, int nz, int nr, int nc, double* picks, cudaStream_t st);

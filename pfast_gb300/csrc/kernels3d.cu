@@ -433,6 +433,9 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     constexpr bool kPrune = KIND != kFwdPlain64 && KIND != kAdjPlain64;
     bool m_klo = false, m_khi = false, m_ilo = false, m_ihi = false;
     bool restep = false;   // polish: some update left a remainder above the floor (visit again in this order)
+    // FP32 bulk: some changed node feeds an in-tile node that this pass visited before it
+    // (so the tile is not yet a fixed point of the update)
+    bool stale = false;
 
     // ---- adjoint traveltime windows (FP64 kinds).  Lane (kf, if) (flipped coordinates) is at flipped
     // position jf = t - kf - if in step t and keeps its pencil's traveltimes at jf-1, jf, jf+1
@@ -585,6 +588,13 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                     if (li == ei - 1 && dep(c + HJ, Typ)) m_ihi = true;
                     if (lj == 0 && dep(c - 1, Txm)) chg_jlo = true;
                     if (lj == ej - 1 && dep(c + 1, Txp)) chg_jhi = true;
+                    if constexpr (!kSelective) {
+                        // the in-tile neighbours this pass visited before the node (one step
+                        // back along each flipped axis)
+                        if (lkf > 0 && dep(pz ? c - PS : c + PS, pz ? Tzm : Tzp)) stale = true;
+                        if (lif > 0 && dep(py ? c - HJ : c + HJ, py ? Tym : Typ)) stale = true;
+                        if (ljf > 0 && dep(px ? c - 1 : c + 1, px ? Txm : Txp)) stale = true;
+                    }
                 } else {
                     if (lj == 0) chg_jlo = true;
                     if (lj == ej - 1) chg_jhi = true;
@@ -613,15 +623,20 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     const unsigned f_ihi = __ballot_sync(0xffffffffu, kPrune ? m_ihi : chg && li == ei - 1);
     const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
     const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
-    // A polish sweep in order o leaves every node that selects o consistent with the values
-    // it reads (its active neighbours come before it in o), so after small updates the tile
-    // is due again in o only when a neighbour or another order changes something.
-    const bool again = !kSelective || __any_sync(0xffffffffu, restep);
+    // Own re-marking.  A polish sweep in order o leaves every node that selects o consistent
+    // with the values it reads (its active neighbours come before it in o), so after small
+    // updates the tile is due again in o only when a neighbour or another order changes
+    // something.  An FP32 bulk pass in which no changed node feeds an already visited node
+    // leaves the tile a fixed point of the update: it stays locked until a neighbour marks it.
+    // The plain kinds re-mark all orders (their tile skipping must stay exact).
+    bool again = true;
+    if constexpr (kSelective) again = __any_sync(0xffffffffu, restep);
+    else if constexpr (kPrune) again = __any_sync(0xffffffffu, stale);
     if (lane == 0) {
         // neighbours keep their selection bits: OR in the eight order bits (two tiles of one
         // launch can share a face neighbour, hence atomic)
         const int sk_ = A.nbi * A.nbj;
-        dirty[tid] |= again ? 0xff : (0xff & ~obit);
+        dirty[tid] |= again ? 0xff : (kSelective ? (0xff & ~obit) : 0);
         if (f_klo && tk > 0) atomicOr(dirty + tid - sk_, 0xff);
         if (f_khi && tk < A.nbk - 1) atomicOr(dirty + tid + sk_, 0xff);
         if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xff);
@@ -754,43 +769,42 @@ __global__ void __launch_bounds__(kMaxPWarps * 32) sweep3d_persistent(const Swee
 // Polish pre-pass: lock word of every tile = all eight orders due | (orders in which some node
 // of the tile is selected) << 8, the selection computed from the field the polish starts
 // from (forward: the widened bulk traveltimes; adjoint: the fixed traveltimes), so that the
-// first polish sweep skips the tiles none of whose nodes it selects.  One thread per node;
-// the lanes of a warp that share a tile OR their masks and one of them ORs it in.
+// first polish sweep skips the tiles none of whose nodes it selects.  One warp per tile
+// (lane = column, looping over the tile's rows) writes the tile's lock word.
 template <bool ADJ>
 __global__ void tile_orders_kernel(const Sweep3Args A) {
+    const int tid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (tid >= A.ntiles) return;   // whole warps
     const int inst = A.act[blockIdx.y];
-    const int nz = A.nz, nr = A.nr, nc = A.nc;
-    const long long plane = (long long)nr * nc, N = plane * nz;
-    const double* f = reinterpret_cast<const double*>(ADJ ? A.aux : A.field) + inst * A.fstride;
     const int lane = threadIdx.x & 31;
+    const int nz = A.nz, nr = A.nr, nc = A.nc;
+    const long long plane = (long long)nr * nc;
+    const double* f = reinterpret_cast<const double*>(ADJ ? A.aux : A.field) + inst * A.fstride;
+    const int tj = tid % A.nbj, ti = (tid / A.nbj) % A.nbi, tk = tid / (A.nbj * A.nbi);
+    const int k0 = tk * TK, i0 = ti * TI, j = tj * TJ + lane;
     int sk = 0, si = 0, sj = 0;
     if (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
     const long long inf = dbits(INFINITY);
-    const long long step = (long long)gridDim.x * blockDim.x;
-    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x - lane); base < N; base += step) {
-        const long long t = base + lane;
-        const bool valid = t < N;
-        unsigned m = 0;
-        int tid = -1;
-        if (valid) {
-            const int k = (int)(t / plane), i = (int)((t / nc) % nr), j = (int)(t % nc);
-            tid = ((k / TK) * A.nbi + i / TI) * A.nbj + j / TJ;
-            const long long xl = j > 0 ? dbits(f[t - 1]) : inf, xh = j < nc - 1 ? dbits(f[t + 1]) : inf;
-            const long long yl = i > 0 ? dbits(f[t - nc]) : inf, yh = i < nr - 1 ? dbits(f[t + nc]) : inf;
-            const long long zl = k > 0 ? dbits(f[t - plane]) : inf, zh = k < nz - 1 ? dbits(f[t + plane]) : inf;
-            if constexpr (ADJ) {
-                const bool interior = k >= 1 && k <= nz - 2 && i >= 1 && i <= nr - 2 && j >= 1 && j <= nc - 2;
-                const bool fixed = (A.mask[inst * A.mask_stride + ((long long)k * nr + i) * A.wpr + (j >> 5)] >> (j & 31)) & 1u;
-                if (interior && !fixed) m = adj_orders(dbits(f[t]), xl, xh, yl, yh, zl, zh);
-            } else {
-                const int qk = k - sk, qi = i - si, qj = j - sj;
-                if (qk * qk + qi * qi + qj * qj > A.src_r2) m = fwd_orders(dbits(f[t]), xl, xh, yl, yh, zl, zh);
-            }
+    unsigned m = 0;
+#pragma unroll 1
+    for (int r = 0; r < TK * TI; ++r) {
+        const int k = k0 + r / TI, i = i0 + r % TI;
+        if (k >= nz || i >= nr || j >= nc) continue;
+        const long long t = k * plane + (long long)i * nc + j;
+        const long long xl = j > 0 ? dbits(__ldg(f + t - 1)) : inf, xh = j < nc - 1 ? dbits(__ldg(f + t + 1)) : inf;
+        const long long yl = i > 0 ? dbits(__ldg(f + t - nc)) : inf, yh = i < nr - 1 ? dbits(__ldg(f + t + nc)) : inf;
+        const long long zl = k > 0 ? dbits(__ldg(f + t - plane)) : inf, zh = k < nz - 1 ? dbits(__ldg(f + t + plane)) : inf;
+        if constexpr (ADJ) {
+            const bool interior = k >= 1 && k <= nz - 2 && i >= 1 && i <= nr - 2 && j >= 1 && j <= nc - 2;
+            const bool fixed = (A.mask[inst * A.mask_stride + ((long long)k * nr + i) * A.wpr + (j >> 5)] >> (j & 31)) & 1u;
+            if (interior && !fixed) m |= adj_orders(dbits(__ldg(f + t)), xl, xh, yl, yh, zl, zh);
+        } else {
+            const int qk = k - sk, qi = i - si, qj = j - sj;
+            if (qk * qk + qi * qi + qj * qj > A.src_r2) m |= fwd_orders(dbits(__ldg(f + t)), xl, xh, yl, yh, zl, zh);
         }
-        const unsigned grp = __match_any_sync(0xffffffffu, tid);
-        const unsigned om = __reduce_or_sync(grp, m);
-        if (valid && om && lane == __ffs(grp) - 1) atomicOr(A.dirty + (long long)inst * A.ntiles + tid, (int)(om << 8));
     }
+    m = __reduce_or_sync(0xffffffffu, m);
+    if (lane == 0) A.dirty[(long long)inst * A.ntiles + tid] = 0xff | (int)(m << 8);
 }
 
 __global__ void fill_int_kernel(int* __restrict__ p, long long n, int v) {
@@ -967,8 +981,7 @@ pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int na
     if (nact <= 0) return PFAST_OK;
     const long long n = (long long)a.ntiles * nb;
     fill_int_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 32), 256, 0, st>>>(a.dirty, n, 0xff);
-    const long long N = (long long)a.nz * a.nr * a.nc;
-    dim3 grid((unsigned)std::min<long long>((N + 255) / 256, 152LL * 8), nact);
+    dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
     if (kind == kAdjPolish64) tile_orders_kernel<true><<<grid, 256, 0, st>>>(a);
     else tile_orders_kernel<false><<<grid, 256, 0, st>>>(a);
     cudaError_t e = cudaGetLastError();
@@ -1125,13 +1138,23 @@ __global__ void bc3_kernel(const Bc3Args A) {
     }
 }
 
+// g -= lambda_b / v^3 over the batch's sources.  exact: one division per source, in source
+// order, as the reference accumulates (src/T_PFAST3D.cpp:393).  Otherwise the sources'
+// lambdas are summed first and divided once (the mixed-precision path: FP64 divisions are
+// scarce on this part and the reassociation is far below its tolerance).
 __global__ void accumulate_kernel(double* __restrict__ g, const double* __restrict__ lam, long long fstride,
-                                  const double* __restrict__ vp, long long n, int nb) {
+                                  const double* __restrict__ vp, long long n, int nb, int exact) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         const double v = vp[t];
         const double v3 = v * v * v;
         double acc = g[t];
-        for (int b = 0; b < nb; ++b) acc = acc - lam[b * fstride + t] / v3;   // src/T_PFAST3D.cpp:393
+        if (exact) {
+            for (int b = 0; b < nb; ++b) acc = acc - lam[b * fstride + t] / v3;
+        } else {
+            double sum = 0.0;
+            for (int b = 0; b < nb; ++b) sum += __ldcs(lam + b * fstride + t);
+            acc = acc - sum / v3;
+        }
         g[t] = acc;
     }
 }
@@ -1218,8 +1241,8 @@ pfast_status launch_bc3(const Bc3Args& a, int nbatch, cudaStream_t st) {
 }
 
 pfast_status launch_accumulate(double* grad, const double* lam, long long fstride, const double* vp, long long n,
-                               int nbatch, cudaStream_t st) {
-    accumulate_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, lam, fstride, vp, n, nbatch);
+                               int nbatch, bool exact, cudaStream_t st) {
+    accumulate_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, lam, fstride, vp, n, nbatch, exact ? 1 : 0);
     PFAST_LAUNCH_CHECK();
     return PFAST_OK;
 }
