@@ -301,7 +301,7 @@ def main():
     # DRAM bytes per launch of the polish kernels, measured with ncu (dram__bytes_read.sum +
     # dram__bytes_write.sum over the 1680 launches of one evaluation on the 9-source case of this
     # grid), per source of a launch; a launch's traffic grows with the sources it carries.
-    traffic_per_src = {"fwd64": 0.404e6, "adj64": 0.461e6}
+    traffic_per_src = {"fwd64": 0.279e6, "adj64": 0.347e6}
     traffic = traffic_per_src[dom] * len(srnum) if dom in traffic_per_src else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_unit": "bytes per launch",
