@@ -267,7 +267,8 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
             }
         }
         PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));
-        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.ntiles, a.act, nact, a.changed, st));
+        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 8, 0xff,
+                                             a.ntiles, a.act, nact, a.changed, st));
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) return cuda_fail(le, "sweep launch", __FILE__, __LINE__);
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
@@ -277,7 +278,12 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
         still.reserve(nact);
         for (int id : active) {
             iters[id] = it;
-            if (h_chg[id]) still.push_back(id);
+            if (!(h_chg[id] & 1)) continue;   // converged: no node moved by more than the tolerance
+            // Moved, but no tile is due in any order: every tile is a fixed point of its update
+            // (tile locking), so the next outer iteration would change nothing and pass the
+            // convergence test.  It is counted without being launched.
+            if (!(h_chg[id] & 2) && it < maxiter) { iters[id] = it + 1; continue; }
+            still.push_back(id);
         }
         active.swap(still);
     }
@@ -784,6 +790,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
         if (picks) PFAST_LAUNCH(ctx, launch_gather3(ctx->T64.as<double>(), N, sv->d_rec, sv->d_ch0 + b0, sv->d_srnum + b0, nb,
                                             sv->nz, sv->nr, sv->nc, picks, s));
     }
+    if (want_grad && o.precision != PFAST_PLAIN_FP64) PFAST_LAUNCH(ctx, launch_finish_gradient(grad, vp, N, s));
     PFAST_CUDA_TRY(cudaEventRecord(t1, s));
     PFAST_CUDA_TRY(cudaStreamSynchronize(s));
     if (stats) {

@@ -127,7 +127,8 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
             }
         }
         PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * ninst, st));
-        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.ntiles, a.act, nact, a.changed, st));
+        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 4, 0xf,
+                                             a.ntiles, a.act, nact, a.changed, st));
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) return cuda_fail(le, "sweep2 launch", __FILE__, __LINE__);
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * ninst, cudaMemcpyDeviceToHost, st));
@@ -136,9 +137,15 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
         std::vector<int> still;
         for (int q : active) {
             iters[q] = it;
-            if (h_chg[q]) {
-                if (it < caps[q]) still.push_back(q);
-                else if (not_conv) ++*not_conv;
+            if (h_chg[q] & 1) {
+                if (it < caps[q]) {
+                    // moved, but every tile locked: the next iteration would change nothing and
+                    // pass the convergence test; it is counted without being launched
+                    if (!(h_chg[q] & 2)) iters[q] = it + 1;
+                    else still.push_back(q);
+                } else if (not_conv) {
+                    ++*not_conv;
+                }
             }
         }
         active.swap(still);

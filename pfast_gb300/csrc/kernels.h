@@ -57,8 +57,11 @@ pfast_status build_diag_table3(int nz, int nr, int nc, DiagTable3& t);
 void free_diag_table3(DiagTable3& t);
 
 size_t sweep3_smem_bytes(int kind);
-// changed[act[b]] = any diff over the tiles of instance act[b], b < nact.
-pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
+// changed[act[b]], b < nact: bit 0 = any diff over the tiles of instance act[b]; bit 1 = some
+// tile still due in some order (lock words `dirty`: order bits order_mask, selected orders
+// `shift` bits higher for the selective polish kinds).
+pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selective, int shift, int order_mask,
+                                int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
 // Polish kinds: initial lock words (every order due, the tile's selected orders in bits 8-15),
 // computed from a.field (forward) or a.aux (adjoint) for the nb instances (a.act lists nact).
 pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int nact, cudaStream_t st);
@@ -106,9 +109,12 @@ struct Bc3Args {
 };
 pfast_status launch_bc3(const Bc3Args& a, int nbatch, cudaStream_t st);
 
-// grad[n] <- grad[n] - lam_b[n] / (v*v*v), b = 0..nbatch-1 in order (src/T_PFAST3D.cpp:393).
+// exact: grad[n] <- grad[n] - lam_b[n] / (v*v*v), b = 0..nbatch-1 in order (src/T_PFAST3D.cpp:393);
+// otherwise grad[n] <- grad[n] + lam_b[n] in order (running sum, finished by launch_finish_gradient).
 pfast_status launch_accumulate(double* grad, const double* lam, long long fstride, const double* vp, long long n,
                                int nbatch, bool exact, cudaStream_t st);
+// g = -g / v^3: the mixed-precision path's single division after its running lambda sum.
+pfast_status launch_finish_gradient(double* grad, const double* vp, long long n, cudaStream_t st);
 // picks[row] = T_b[rec[row]] for rows of each batch source.
 pfast_status launch_gather3(const double* T, long long fstride, const int* rec, const int* ch0, const int* srnum,
                             int nbatch, int nz, int nr, int nc, double* picks, cudaStream_t st);

@@ -812,15 +812,24 @@ __global__ void fill_int_kernel(int* __restrict__ p, long long n, int v) {
         p[t] = v;
 }
 
-// changed[act[b]] = OR over the tiles of instance act[b] of diff.
-__global__ void reduce_diff_kernel(const int* __restrict__ diff, int ntiles, const int* __restrict__ act,
+// changed[act[b]] bit 0 = OR over the tiles of instance act[b] of diff; bit 1 = some tile
+// is still due in some order (its lock word: the order bits `order_mask`; selective kinds
+// hold the selected orders `shift` bits higher, and an order counts when due and selected).
+__global__ void reduce_diff_kernel(const int* __restrict__ diff, const int* __restrict__ dirty, int selective,
+                                   int shift, int order_mask, int ntiles, const int* __restrict__ act,
                                    int* __restrict__ changed) {
     const int inst = act[blockIdx.x];
     const int* d = diff + (long long)inst * ntiles;
-    int any = 0;
-    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) any |= d[t];
+    const int* w = dirty + (long long)inst * ntiles;
+    int any = 0, due = 0;
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+        any |= d[t];
+        const int dm = w[t];
+        due |= (selective ? (dm & (dm >> shift)) : dm) & order_mask;
+    }
     any = __syncthreads_or(any);
-    if (threadIdx.x == 0) changed[inst] = any ? 1 : 0;
+    due = __syncthreads_or(due);
+    if (threadIdx.x == 0) changed[inst] = (any ? 1 : 0) | (due ? 2 : 0);
 }
 
 }  // namespace
@@ -989,9 +998,10 @@ pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int na
     return PFAST_OK;
 }
 
-pfast_status launch_reduce_diff(const int* diff, int ntiles, const int* act, int nact, int* changed, cudaStream_t st) {
+pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selective, int shift, int order_mask,
+                                int ntiles, const int* act, int nact, int* changed, cudaStream_t st) {
     if (nact <= 0) return PFAST_OK;
-    reduce_diff_kernel<<<nact, 256, 0, st>>>(diff, ntiles, act, changed);
+    reduce_diff_kernel<<<nact, 256, 0, st>>>(diff, dirty, selective ? 1 : 0, shift, order_mask, ntiles, act, changed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "reduce_diff launch", __FILE__, __LINE__);
     return PFAST_OK;
@@ -1138,24 +1148,31 @@ __global__ void bc3_kernel(const Bc3Args A) {
     }
 }
 
-// g -= lambda_b / v^3 over the batch's sources.  exact: one division per source, in source
-// order, as the reference accumulates (src/T_PFAST3D.cpp:393).  Otherwise the sources'
-// lambdas are summed first and divided once (the mixed-precision path: FP64 divisions are
-// scarce on this part and the reassociation is far below its tolerance).
+// exact: g -= lambda_b / v^3 over the batch's sources, one division per source in source
+// order, as the reference accumulates (src/T_PFAST3D.cpp:393).  Otherwise (the mixed-precision
+// path: FP64 divisions are scarce on this part) g holds the running sum of lambda over the
+// sources, added in source order, so the sum does not depend on how the sources are split into
+// batches; finish_gradient_kernel divides once at the end.
 __global__ void accumulate_kernel(double* __restrict__ g, const double* __restrict__ lam, long long fstride,
                                   const double* __restrict__ vp, long long n, int nb, int exact) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const double v = vp[t];
-        const double v3 = v * v * v;
         double acc = g[t];
         if (exact) {
+            const double v = vp[t];
+            const double v3 = v * v * v;
             for (int b = 0; b < nb; ++b) acc = acc - lam[b * fstride + t] / v3;
         } else {
-            double sum = 0.0;
-            for (int b = 0; b < nb; ++b) sum += __ldcs(lam + b * fstride + t);
-            acc = acc - sum / v3;
+            for (int b = 0; b < nb; ++b) acc += __ldcs(lam + b * fstride + t);
         }
         g[t] = acc;
+    }
+}
+
+// g = -(sum of lambda) / v^3 after the last batch of the mixed-precision path.
+__global__ void finish_gradient_kernel(double* __restrict__ g, const double* __restrict__ vp, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double v = vp[t];
+        g[t] = 0.0 - g[t] / (v * v * v);
     }
 }
 
@@ -1243,6 +1260,12 @@ pfast_status launch_bc3(const Bc3Args& a, int nbatch, cudaStream_t st) {
 pfast_status launch_accumulate(double* grad, const double* lam, long long fstride, const double* vp, long long n,
                                int nbatch, bool exact, cudaStream_t st) {
     accumulate_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, lam, fstride, vp, n, nbatch, exact ? 1 : 0);
+    PFAST_LAUNCH_CHECK();
+    return PFAST_OK;
+}
+
+pfast_status launch_finish_gradient(double* grad, const double* vp, long long n, cudaStream_t st) {
+    finish_gradient_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, vp, n);
     PFAST_LAUNCH_CHECK();
     return PFAST_OK;
 }

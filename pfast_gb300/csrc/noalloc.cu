@@ -198,12 +198,13 @@ extern "C" pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src
             }
         }
         PFAST_CUDA_TRY(cudaMemsetAsync(d_changed, 0, sizeof(int), s));
-        r = launch_reduce_diff(a.diff, ntiles, d_act, 1, d_changed, s);
+        r = launch_reduce_diff(a.diff, a.dirty, false, 8, 0xff, ntiles, d_act, 1, d_changed, s);
         if (r) return r;
         int changed = 0;
         PFAST_CUDA_TRY(cudaMemcpyAsync(&changed, d_changed, sizeof(int), cudaMemcpyDeviceToHost, s));
         PFAST_CUDA_TRY(cudaStreamSynchronize(s));
-        if (!changed) break;
+        // converged, or moved with every tile locked (the next iteration would change nothing)
+        if (!(changed & 1) || !(changed & 2)) break;
     }
     PFAST_CUDA_TRY(cudaStreamSynchronize(s));   // the host table vectors are read by the copies above
     return PFAST_OK;
