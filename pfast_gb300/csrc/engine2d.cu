@@ -172,6 +172,10 @@ Sweep2Args base2(const pfast_survey2d* sv) {
     a.inv2z = 1.0 / sv->dz / sv->dz;
     a.dxf = (float)sv->dx;
     a.dzf = (float)sv->dz;
+    a.wxf = (float)a.inv2x;
+    a.wzf = (float)a.inv2z;
+    a.rsumf = (float)(1.0 / (a.inv2x + a.inv2z));
+    a.polish_floor = kPolishFloor;
     a.wpr = (sv->nc + 31) / 32;
     return a;
 }

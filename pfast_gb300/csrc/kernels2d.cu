@@ -102,29 +102,51 @@ __device__ __forceinline__ float adj2_bulk(float T0, float Txp, float Txm, float
     return (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
 }
 
+// FP64 polish adjoint update in residual-correction form (see kernels3d.cu): with mu_m =
+// lambda_m where e_m > 0 and lambda0 where e_m < 0, r = num - den*lambda0 = sum_m w_m e_m mu_m
+// in FP64 (11 FP64 instructions); den only scales the step and is FP32.  big: the FP32 step
+// leaves a remainder above the floor.
 __device__ __forceinline__ double adj2_polish(double T0, double Txp, double Txm, double Tzp, double Tzm, double Lxp,
-                                              double Lxm, double Lzp, double Lzm, double L0, double wx, double wz) {
-    if (Txp >= kInf || T0 >= kInf || Txm >= kInf || Tzp >= kInf || Tzm >= kInf) return 0.0;
-    double num, den;
-    adj2_terms<double>(T0, Txp, Txm, Tzp, Tzm, Lxp, Lxm, Lzp, Lzm, wx, wz, num, den);
-    if (!(fabs(den) > 1e-9)) return 0.0;
-    const double r = fma(-den, L0, num);
-    const float step = __fdividef((float)r, (float)den);
+                                              double Lxm, double Lzp, double Lzm, double L0, double wx, double wz,
+                                              float wxf, float wzf, float floor, bool& big) {
+    const long long inf = dbits(kInf);   // T >= INF on the bit patterns (T >= 0)
+    if (dbits(Txp) >= inf || dbits(T0) >= inf || dbits(Txm) >= inf || dbits(Tzp) >= inf || dbits(Tzm) >= inf)
+        return 0.0;
+    const double exp_ = Txp - T0, exm = Txm - T0, ezp = Tzp - T0, ezm = Tzm - T0;
+    auto mu = [&](double e, double L) { return __double2hiint(e) < 0 ? L0 : L; };
+    auto nf = [](double e) { return __double2hiint(e) < 0 ? -narrow_trunc(e) : 0.0f; };   // max(-e, 0)
+    const double r = fma(wx, fma(exp_, mu(exp_, Lxp), exm * mu(exm, Lxm)),
+                         wz * fma(ezp, mu(ezp, Lzp), ezm * mu(ezm, Lzm)));
+    const float den = wxf * (nf(exp_) + nf(exm)) + wzf * (nf(ezp) + nf(ezm));
+    if (!(den > 1e-9f)) return 0.0;
+    const float step = __fdividef(narrow_trunc(r), den);
+    const float tol = floor * (1.0f + fabsf(narrow_trunc(L0)));
+    big = fabsf(step) * 1.2e-7f > tol;
     // corrections far below the convergence tolerance are dropped (bitwise fixed point, tiles lock)
-    return fabsf(step) <= kPolishFloor * (1.0f + fabsf((float)L0)) ? L0 : L0 + (double)step;
+    return fabsf(step) <= tol ? L0 : L0 + widen_exact(step);
 }
 
 // FP64 polish Godunov update, one Newton step on f(q) = wx max(q-a,0)^2 + wz max(q-b,0)^2 - s^2
-// (FP64 residual, FP32 step); a: x-neighbour minimum, b: z-neighbour minimum.
+// (FP64 differences and residual, 8 FP64 instructions; FP32 derivative and step); a: x-neighbour
+// minimum, b: z-neighbour minimum.  big: the step's second-order remainder exceeds the floor.
 __device__ __forceinline__ double eik2_newton(double U0, double a, double b, double s, double dx, double dz, double wx,
-                                              double wz) {
-    const double px = fmax(U0 - a, 0.0), pz = fmax(U0 - b, 0.0);
+                                              double wz, float wxf, float wzf, float floor, bool& big) {
+    const double px = pos_sign(U0 - a), pz = pos_sign(U0 - b);
     const double f = fma(wx * px, px, fma(wz * pz, pz, -s * s));
-    const float fp = 2.0f * ((float)wx * (float)px + (float)wz * (float)pz);
-    if (!(fp > 0.0f)) return fmin(fma(dx, s, a), fma(dz, s, b));
-    const float step = __fdividef((float)f, fp);
-    return fabsf(step) <= kPolishFloor ? U0 : U0 - (double)step;   // bitwise fixed point once converged
+    const float fp = 2.0f * (wxf * narrow_trunc(px) + wzf * narrow_trunc(pz));
+    if (!(fp > 0.0f)) {
+        big = true;
+        return fmin(fma(dx, s, a), fma(dz, s, b));
+    }
+    const float step = __fdividef(narrow_trunc(f), fp);
+    const float sw = (dbits(px) > 0 ? wxf : 0.0f) + (dbits(pz) > 0 ? wzf : 0.0f);
+    big = sw * step * step > floor * fp;
+    return fabsf(step) <= floor ? U0 : U0 - widen_exact(step);   // bitwise fixed point once converged
 }
+
+// Ordered integer of a value >= 0 (its bit pattern), FP32 or FP64.
+__device__ __forceinline__ long long obits2(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ long long obits2(float x) { return __float_as_int(x); }
 
 // Bitwise equality of two field values (FP32 or FP64).
 template <typename Real>
@@ -272,12 +294,18 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     const Aux* slow = reinterpret_cast<const Aux*>(A.aux);
     const bool row_interior = gi >= 1 && gi <= nr - 2;
 
-    const float wx = float(A.inv2x), wz = float(A.inv2z);
-    const float rsum = float(1.0 / (A.inv2x + A.inv2z));
+    const float wx = A.wxf, wz = A.wzf, rsum = A.rsumf;
     const int cb = (li + 1) * R2 + 1;
     const int steps = ei + ej - 1;
     bool chg = false, chg_jlo = false, chg_jhi = false;
     unsigned sel = 0;
+    // Face marks and own re-marking as in the 3D sweeps: the plain kinds mark every changed
+    // face node; the others only where the neighbour's node depends on the changed one (forward:
+    // a neighbour below the node's value; adjoint: a larger traveltime).
+    constexpr bool kPrune = KIND != kFwdPlain64 && KIND != kAdjPlain64;
+    bool m_ilo = false, m_ihi = false;
+    bool restep = false;   // polish: a remainder above the floor (visit again in this order)
+    bool stale = false;    // FP32 bulk: a changed node feeds an in-tile node visited before it
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
@@ -304,13 +332,30 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         const unsigned m = fwd_orders2(dbits(old), dbits(box[c - 1]), dbits(box[c + 1]),
                                                        dbits(box[c - R2]), dbits(box[c + R2]));
                         sel |= m;
-                        if (m & obit) nv = eik2_newton(old, ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z);
+                        if (m & obit) {
+                            bool big = false;
+                            nv = eik2_newton(old, ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z, A.wxf, A.wzf,
+                                             A.polish_floor, big);
+                            restep |= big;
+                        }
                     }
                     if (!bits_same(old, nv)) {
                         box[c] = nv;
                         chg = true;
-                        if (lj == 0) chg_jlo = true;
-                        if (lj == ej - 1) chg_jhi = true;
+                        if constexpr (kPrune) {
+                            auto dep = [&](int n) { return min(obits2(old), obits2(nv)) < obits2(box[n]); };
+                            if (li == 0 && dep(c - R2)) m_ilo = true;
+                            if (li == ei - 1 && dep(c + R2)) m_ihi = true;
+                            if (lj == 0 && dep(c - 1)) chg_jlo = true;
+                            if (lj == ej - 1 && dep(c + 1)) chg_jhi = true;
+                            if constexpr (!kSelective) {
+                                if (lif > 0 && dep(py ? c - R2 : c + R2)) stale = true;
+                                if (ljf > 0 && dep(px ? c - 1 : c + 1)) stale = true;
+                            }
+                        } else {
+                            if (lj == 0) chg_jlo = true;
+                            if (lj == ej - 1) chg_jhi = true;
+                        }
                     }
                 }
             } else {
@@ -328,15 +373,36 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         const unsigned m = adj_orders2(dbits(tbox[c]), dbits(tbox[c - 1]), dbits(tbox[c + 1]),
                                                        dbits(tbox[c - R2]), dbits(tbox[c + R2]));
                         sel |= m;
-                        if (m & obit)
+                        if (m & obit) {
+                            bool big = false;
                             r = adj2_polish(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
-                                            box[c - 1], box[c + R2], box[c - R2], old, A.inv2x, A.inv2z);
+                                            box[c - 1], box[c + R2], box[c - R2], old, A.inv2x, A.inv2z, A.wxf,
+                                            A.wzf, A.polish_floor, big);
+                            restep |= big;
+                        }
                     }
                     if (!bits_same(old, r)) {
                         box[c] = r;
                         chg = true;
-                        if (lj == 0) chg_jlo = true;
-                        if (lj == ej - 1) chg_jhi = true;
+                        if constexpr (kPrune) {
+                            // lambda at the neighbour node reads this node if its traveltime is larger
+                            // (FP32 bulk: offsets from the tile's corner, compared as values)
+                            auto dep = [&](int n) {
+                                if constexpr (sizeof(Aux) == 8) return obits2(tbox[c]) > obits2(tbox[n]);
+                                else return tbox[c] > tbox[n];
+                            };
+                            if (li == 0 && dep(c - R2)) m_ilo = true;
+                            if (li == ei - 1 && dep(c + R2)) m_ihi = true;
+                            if (lj == 0 && dep(c - 1)) chg_jlo = true;
+                            if (lj == ej - 1 && dep(c + 1)) chg_jhi = true;
+                            if constexpr (!kSelective) {
+                                if (lif > 0 && dep(py ? c - R2 : c + R2)) stale = true;
+                                if (ljf > 0 && dep(px ? c - 1 : c + 1)) stale = true;
+                            }
+                        } else {
+                            if (lj == 0) chg_jlo = true;
+                            if (lj == ej - 1) chg_jhi = true;
+                        }
                     }
                 }
             }
@@ -351,12 +417,18 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     // nothing changed: field and snapshot comparison stand as they are
     if (!__any_sync(0xffffffffu, chg)) return;
     // unlock this tile and the face neighbours that see a changed face node (lane = row)
-    const unsigned f_ilo = __ballot_sync(0xffffffffu, chg && li == 0);
-    const unsigned f_ihi = __ballot_sync(0xffffffffu, chg && li == ei - 1);
+    const unsigned f_ilo = __ballot_sync(0xffffffffu, kPrune ? m_ilo : chg && li == 0);
+    const unsigned f_ihi = __ballot_sync(0xffffffffu, kPrune ? m_ihi : chg && li == ei - 1);
     const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
     const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
+    // own re-marking (see the 3D sweeps): a polish tile stays locked in this order after
+    // updates with remainders below the floor; an FP32 bulk tile none of whose changed nodes
+    // feeds an already visited node is a fixed point until a neighbour marks it
+    bool again = true;
+    if constexpr (kSelective) again = __any_sync(0xffffffffu, restep);
+    else if constexpr (kPrune) again = __any_sync(0xffffffffu, stale);
     if (lane == 0) {
-        dirty[tid] |= 0xf;
+        dirty[tid] |= again ? 0xf : (kSelective ? (0xf & ~obit) : 0);
         if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xf);
         if (f_ihi && ti < A.nbi - 1) atomicOr(dirty + tid + A.nbj, 0xf);
         if (f_jlo && tj > 0) atomicOr(dirty + tid - 1, 0xf);

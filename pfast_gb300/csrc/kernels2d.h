@@ -32,6 +32,8 @@ struct Sweep2Args {
     double dx, dz;
     double inv2x, inv2z;         // (1.0/dx)/dx, (1.0/dz)/dz
     float dxf, dzf;              // FP32 copies of dx, dz (no FP64 instruction in the FP32 sweeps)
+    float wxf, wzf, rsumf;       // FP32 inv2x, inv2z, 1/(inv2x + inv2z)
+    float polish_floor;          // polish corrections at or below this are dropped
     int dir;                     // 0..3: bit1 = s1>0 (rows), bit0 = s2>0 (cols); reference order
     int iter;                    // outer iteration (snapshot stamps)
     int ntiles;                  // tiles per instance (nbi * nbj)

@@ -107,16 +107,22 @@ def test_survey_eval_plain_bit_exact(ctx, shape, h, seed):
     assert bits_equal(picks.cpu().numpy(), want)
 
 
-def test_batch_split_does_not_change_bits(ctx):
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_batch_split_does_not_change_bits(ctx, precision):
+    # plain: one division per source in source order; mixed: the running lambda sum in source
+    # order and one division at the end -- either way the split into batches changes no bit
     pg, torch = _pg(), _torch()
+    prec = pg.PFAST_PLAIN_FP64 if precision == "plain" else pg.PFAST_MIXED
     shape, h = (10, 21, 70), (20.0, 20.0, 20.0)
     vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 7)
     sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src, srnum, rec, nxyz, tobs)
     d = torch.from_numpy(vp).cuda()
-    g_all, e_all, _ = sv.eval(d)
-    g_one, e_one, st = sv.eval(d, max_batch=1)
-    assert st["batches"] == 3
+    g_all, e_all, _ = sv.eval(d, precision=prec)
+    g_one, e_one, st = sv.eval(d, precision=prec, max_batch=1)
+    g_two, e_two, st2 = sv.eval(d, precision=prec, max_batch=2)
+    assert st["batches"] == 3 and st2["batches"] == 2
     assert bits_equal(g_all.cpu().numpy(), g_one.cpu().numpy()) and e_all == e_one
+    assert bits_equal(g_all.cpu().numpy(), g_two.cpu().numpy()) and e_all == e_two
 
 
 @pytest.mark.parametrize("maxswp", [1, 2])
