@@ -111,6 +111,27 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def fp64_peak_gflops(n=4096, reps=3):
+    """Dense FP64 rate of this GPU: a cuBLAS DGEMM (torch.matmul on float64 n^3, 2 n^3 flops),
+    best of `reps` after a warm-up, timed with CUDA events.  The polish kernels' FP64 roof."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best / 1e3) / 1e9
+
+
 def cpu_eval_sample(vt, v0, src, srnum, rec, nxyz, nsample, nthreads, seed):
     """The oracle port (CPU restatement) on `nsample` sources: picks on the true model + noise
     (untimed), then one timed misfit+gradient evaluation.  Returns (evals/s, seconds)."""
@@ -214,7 +235,9 @@ def main():
     d_vp = torch.from_numpy(v0).cuda()
     grad = torch.empty_like(d_vp)
 
-    # ---- schedule autotuning on this workload (both schedules once, same bits), then warm-up
+    # ---- the FP64 roof (a DGEMM, before anything is timed), schedule autotuning on this
+    # workload (both schedules once, same bits), then warm-up
+    fp64_gflops = fp64_peak_gflops() if rank == 0 else None
     tune = sv.autotune(d_vp, precision=pg.PFAST_MIXED)
     # ---- device-resident timing (inputs already in HBM)
     for _ in range(args.warmup):
@@ -289,6 +312,9 @@ def main():
               "adj64": (st["ms_adj64"], st["adj64_node_updates"], 8, "sweep3d_kernel<kAdjPolish64>")}
     dom = max(phases, key=lambda k: phases[k][0])
     ms_dom, upd_dom, w, kname = phases[dom]
+    # FP64 instructions per executed node update of the polish kernels (the residual-form
+    # updates; everything else in them runs on the integer and FP32 pipes)
+    fp64_per_update = {"fwd32": 0, "fwd64": 8, "adj32": 0, "adj64": 13}[dom]
     alg_bytes = upd_dom * 3 * w                       # read U + read slowness/T + write U per node update
     # launches of that kernel per evaluation: outer iterations x 8 sweep orders x tile diagonals
     # (4 x 8 x 32 tiles: nbk + nbi + nbj - 2 diagonals)
@@ -309,6 +335,15 @@ def main():
                 "kernel": kname, "phase": dom,
                 "peak_kind": peak_kind, "node_updates_per_s": upd_dom / (ms_dom / 1e3) if ms_dom > 0 else 0.0,
                 "phase_ms": ms_dom}
+    if fp64_per_update and ms_dom > 0 and fp64_gflops:
+        # FP64 roof: FP64 instructions of the executed updates per second against the DGEMM rate
+        # in FMA instructions per second (an FMA is one instruction, two flops).  A lower bound
+        # of the FP64 pipe's occupancy: an FP64 warp instruction holds the pipe for ~75 cycles
+        # however many of its lanes are active, and wavefront steps run with idle lanes.
+        ach = upd_dom * fp64_per_update / (ms_dom / 1e3) / 1e9
+        roofline["fp64"] = {"per_update": fp64_per_update, "achieved": ach, "peak": fp64_gflops / 2.0,
+                            "unit": "G FP64 instructions/s", "frac": ach / (fp64_gflops / 2.0),
+                            "peak_kind": "measured: cuBLAS DGEMM 4096^3 through torch, best of 3, FMA = 1 instruction"}
 
     # ---- CPU baseline (oracle port, bounded sample), rank 0 at N=1 only
     cpu = None
