@@ -62,9 +62,14 @@ size_t sweep3_smem_bytes(int kind);
 // `shift` bits higher for the selective polish kinds).
 pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selective, int shift, int order_mask,
                                 int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
-// Polish kinds: initial lock words (every order due, the tile's selected orders in bits 8-15),
-// computed from a.field (forward) or a.aux (adjoint) for the nb instances (a.act lists nact).
+// Polish kinds: the tile's initially selected orders in bits 8-15 of its lock word (bits 0-7
+// kept: all orders due, or as seeded), computed from a.field (forward) or a.aux (adjoint) for
+// the active instances a.act[0..nact).
 pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int nact, cudaStream_t st);
+// Initial lock words of the FP32 bulk kinds and the adjoint polish from the starting field
+// (a.field, active instances a.act[0..nact)): 0xff where the tile's halo box holds a reached
+// traveltime / nonzero lambda, else 0.  Other kinds: no-op.
+pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStream_t st);
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
 // Persistent sweep kernel: `blocks` blocks of `warps` warps take the nact instances of a.act
 // from *queue (zeroed by the caller) and solve each to convergence (maxiter outer

@@ -804,13 +804,44 @@ __global__ void tile_orders_kernel(const Sweep3Args A) {
         }
     }
     m = __reduce_or_sync(0xffffffffu, m);
-    if (lane == 0) A.dirty[(long long)inst * A.ntiles + tid] = 0xff | (int)(m << 8);
+    int* w = A.dirty + (long long)inst * A.ntiles + tid;
+    if (lane == 0) *w = (*w & 0xff) | (int)(m << 8);
 }
 
-__global__ void fill_int_kernel(int* __restrict__ p, long long n, int v) {
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        p[t] = v;
+// Initial lock words from the field a phase starts from: a tile is due in every order
+// (0xff) only if its halo box holds a value an update can propagate -- forward: a reached
+// traveltime (below the reference's INF); adjoint: a nonzero lambda -- and locked (0)
+// otherwise.  An update whose neighbours and own value are all unreached (all zero) returns
+// the same value, so such a tile is a fixed point until a neighbour's change marks it.  One
+// warp per tile, lane = column of the box rows.
+template <typename Real, bool ADJ>
+__global__ void seed_tiles_kernel(const Sweep3Args A) {
+    const int tid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (tid >= A.ntiles) return;   // whole warps
+    const int inst = A.act[blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const int nz = A.nz, nr = A.nr, nc = A.nc;
+    const long long plane = (long long)nr * nc;
+    const Real* f = reinterpret_cast<const Real*>(A.field) + inst * A.fstride;
+    const int tj = tid % A.nbj, ti = (tid / A.nbj) % A.nbi, tk = tid / (A.nbj * A.nbi);
+    const int k0 = tk * TK, i0 = ti * TI, j0 = tj * TJ;
+    bool live = false;
+#pragma unroll 1
+    for (int r = 0; r < HK * HI && !live; ++r) {
+        const int k = k0 - 1 + r / HI, i = i0 - 1 + r % HI;
+        if ((unsigned)k >= (unsigned)nz || (unsigned)i >= (unsigned)nr) continue;
+        const Real* row = f + k * plane + (long long)i * nc;
+        bool v = false;
+        for (int j = j0 - 1 + lane; j < j0 + TJ + 1; j += 32) {
+            if ((unsigned)j >= (unsigned)nc) continue;
+            const Real x = __ldg(row + j);
+            v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
+        }
+        live = __any_sync(0xffffffffu, v);
+    }
+    if (lane == 0) A.dirty[(long long)inst * A.ntiles + tid] = live ? 0xff : 0;
 }
+
 
 // changed[act[b]] bit 0 = OR over the tiles of instance act[b] of diff; bit 1 = some tile
 // is still due in some order (its lock word: the order bits `order_mask`; selective kinds
@@ -986,10 +1017,22 @@ pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, i
     return PFAST_ERR_INVALID;
 }
 
+pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStream_t st) {
+    if (nact <= 0) return PFAST_OK;
+    dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
+    switch (kind) {
+        case kFwdFast32: seed_tiles_kernel<float, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjFast32: seed_tiles_kernel<float, true><<<grid, 256, 0, st>>>(a); break;
+        case kAdjPolish64: seed_tiles_kernel<double, true><<<grid, 256, 0, st>>>(a); break;
+        default: return PFAST_OK;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "seed tiles launch", __FILE__, __LINE__);
+    return PFAST_OK;
+}
+
 pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int nact, cudaStream_t st) {
     if (nact <= 0) return PFAST_OK;
-    const long long n = (long long)a.ntiles * nb;
-    fill_int_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 32), 256, 0, st>>>(a.dirty, n, 0xff);
     dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
     if (kind == kAdjPolish64) tile_orders_kernel<true><<<grid, 256, 0, st>>>(a);
     else tile_orders_kernel<false><<<grid, 256, 0, st>>>(a);
