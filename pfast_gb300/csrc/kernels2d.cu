@@ -211,6 +211,35 @@ struct Ident2 {
     template <typename T> __device__ __forceinline__ T operator()(T v) const { return v; }
 };
 
+// Initial lock words from the field a phase starts from (as in the 3D sweeps): a tile is due
+// in every order only if its halo box holds a reached traveltime (forward) or a nonzero lambda
+// (adjoint); otherwise it is a fixed point of the update until a neighbour's change marks it.
+// SEL (polish): an idle tile keeps all four orders selected (bits 4-7), so that a neighbour's
+// mark makes it due.  One warp per tile, lane = column of the box rows.
+template <typename Real, bool ADJ, bool SEL>
+__global__ void seed_tiles2_kernel(const Sweep2Args A) {
+    const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= A.ntiles) return;   // whole warps
+    const int q = A.act[blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const int nr = A.nr, nc = A.nc;
+    const Real* f = reinterpret_cast<const Real*>(A.field) + A.inst_off[q];
+    const int i0 = (t / A.nbj) * T2I, j0 = (t % A.nbj) * T2J;
+    bool live = false;
+#pragma unroll 1
+    for (int i = i0 - 1; i <= i0 + T2I && !live; ++i) {
+        if ((unsigned)i >= (unsigned)nr) continue;
+        bool v = false;
+        for (int j = j0 - 1 + lane; j <= j0 + T2J; j += 32) {
+            if ((unsigned)j >= (unsigned)nc) continue;
+            const Real x = __ldg(f + (long long)i * nc + j);
+            v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
+        }
+        live = __any_sync(0xffffffffu, v);
+    }
+    if (lane == 0) A.dirty[(long long)q * A.ntiles + t] = live ? 0xff : (SEL ? 0xf0 : 0);
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args A, const int d) {
     using Real = typename Traits2<KIND>::Real;
@@ -680,6 +709,20 @@ void free_diag_table2(DiagTable2& t) {
     if (t.d_tiles) cudaFree(t.d_tiles);
     t.d_off = nullptr;
     t.d_tiles = nullptr;
+}
+
+pfast_status launch_seed_tiles2(int kind, const Sweep2Args& a, int nact, cudaStream_t st) {
+    if (nact <= 0) return PFAST_OK;
+    dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
+    switch (kind) {
+        case kFwdFast32: seed_tiles2_kernel<float, false, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjFast32: seed_tiles2_kernel<float, true, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjPolish64: seed_tiles2_kernel<double, true, true><<<grid, 256, 0, st>>>(a); break;
+        default: return PFAST_OK;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "seed tiles2 launch", __FILE__, __LINE__);
+    return PFAST_OK;
 }
 
 pfast_status launch_sweep2(int kind, const Sweep2Args& a, int d, int tiles, int nact, cudaStream_t st) {
