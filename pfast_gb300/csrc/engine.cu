@@ -12,7 +12,6 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
-#include <unordered_set>
 #include <algorithm>
 
 #include "engine.h"
@@ -722,14 +721,13 @@ pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz,
     sv->has_picks = nxyz && T_obs;
     std::vector<unsigned char> last(std::max<long long>(nrec, 1), 0);
     if (sv->has_picks) {
-        for (int s = 0; s < nsrc; ++s) {
-            std::unordered_set<long long> seen;
-            for (int r = sv->h_ch0[s + 1] - 1; r >= sv->h_ch0[s]; --r) {
-                if (!(T_obs[r] < 100)) continue;
-                const long long node = (long long)rec[3 * r + 2] * nrows * ncols + (long long)rec[3 * r] * ncols + rec[3 * r + 1];
-                if (seen.insert(node).second) last[r] = 1;
-            }
-        }
+        std::vector<long long> keys;
+        std::vector<size_t> used;
+        for (int s = 0; s < nsrc; ++s)
+            mark_last_rows(
+                sv->h_ch0[s], sv->h_ch0[s + 1],
+                [&](int r) { return (long long)rec[3 * r + 2] * nrows * ncols + (long long)rec[3 * r] * ncols + rec[3 * r + 1]; },
+                [&](int r) { return T_obs[r] < 100; }, [&](int r) { last[r] = 1; }, keys, used);
     }
     auto up = [&](void** dst, const void* h, size_t bytes) -> pfast_status {
         PFAST_CUDA_TRY(cudaMalloc(dst, std::max<size_t>(bytes, 16)));

@@ -112,6 +112,33 @@ struct pfast_survey2d {
 
 namespace pfast {
 
+// Marks the last row of every node within one source's block of receiver rows [r0, r1):
+// the reference's loops write the receivers in row order, so a node picked twice keeps its
+// later row.  node_of(r) -> node index (>= 0), picked(r) -> whether row r is picked,
+// mark(r) records the row.  A flat open-addressing table (keys, reused across blocks and
+// cleared only where it was written) instead of one hash-set allocation per node.
+template <class NodeOf, class Picked, class Mark>
+void mark_last_rows(int r0, int r1, NodeOf node_of, Picked picked, Mark mark, std::vector<long long>& keys,
+                    std::vector<size_t>& used) {
+    int bits = 4;
+    while ((1ll << bits) < 2ll * (r1 - r0)) ++bits;
+    const size_t cap = (size_t)1 << bits;
+    if (keys.size() < cap) keys.assign(cap, -1);
+    used.clear();
+    for (int r = r1 - 1; r >= r0; --r) {
+        if (!picked(r)) continue;
+        const long long node = node_of(r);
+        size_t h = (size_t)(((unsigned long long)node * 0x9E3779B97F4A7C15ull) >> (64 - bits));
+        while (keys[h] != -1 && keys[h] != node) h = (h + 1) & (cap - 1);
+        if (keys[h] == -1) {
+            keys[h] = node;
+            used.push_back(h);
+            mark(r);
+        }
+    }
+    for (size_t h : used) keys[h] = -1;
+}
+
 pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, DiagTable3** out);
 pfast_status ctx_diag2(pfast_ctx* ctx, int nr, int nc, DiagTable2** out);
 

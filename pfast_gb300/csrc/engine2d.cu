@@ -8,7 +8,6 @@
 
 #include <cstring>
 #include <algorithm>
-#include <unordered_set>
 #include <vector>
 
 #include "engine.h"
@@ -762,19 +761,16 @@ pfast_status pfast_survey2d_create(pfast_ctx* ctx, int nrows, int ncols, double 
     sv->has_picks = nxy && TT_obs && (NumofR == 0 || TR_obs);
     std::vector<unsigned char> last_t(std::max(nrec, 1), 0), last_r(std::max<size_t>((size_t)nrec * NumofR, 1), 0);
     if (sv->has_picks) {
+        std::vector<long long> keys;
+        std::vector<size_t> used;
+        auto node_of = [&](int r) { return (long long)rec[2 * r] * ncols + rec[2 * r + 1]; };
         for (int s = 0; s < nsrc; ++s) {
-            std::unordered_set<long long> seen;
-            for (int r = sv->h_ch0[s + 1] - 1; r >= sv->h_ch0[s]; --r) {
-                if (!(TT_obs[r] < 100)) continue;
-                if (seen.insert((long long)rec[2 * r] * ncols + rec[2 * r + 1]).second) last_t[r] = 1;
-            }
-            for (int ir = 0; ir < NumofR; ++ir) {
-                std::unordered_set<long long> seenr;
-                for (int r = sv->h_ch0[s + 1] - 1; r >= sv->h_ch0[s]; --r) {
-                    if (!(TR_obs[(size_t)r * NumofR + ir] != 0)) continue;
-                    if (seenr.insert((long long)rec[2 * r] * ncols + rec[2 * r + 1]).second) last_r[(size_t)r * NumofR + ir] = 1;
-                }
-            }
+            mark_last_rows(sv->h_ch0[s], sv->h_ch0[s + 1], node_of, [&](int r) { return TT_obs[r] < 100; },
+                           [&](int r) { last_t[r] = 1; }, keys, used);
+            for (int ir = 0; ir < NumofR; ++ir)
+                mark_last_rows(
+                    sv->h_ch0[s], sv->h_ch0[s + 1], node_of, [&](int r) { return TR_obs[(size_t)r * NumofR + ir] != 0; },
+                    [&](int r) { last_r[(size_t)r * NumofR + ir] = 1; }, keys, used);
         }
     }
     auto up = [&](void** dst, const void* h, size_t bytes) -> pfast_status {
