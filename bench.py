@@ -324,13 +324,15 @@ def main():
     launches_dom = iters_dom * 8 * ndiag
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (ms_dom / 1e3) / 1e9 if ms_dom > 0 else 0.0
-    # DRAM bytes per launch of the polish kernels, measured with ncu (dram__bytes_read.sum +
-    # dram__bytes_write.sum over the 1680 launches of one evaluation on the 9-source case of this
-    # grid), per source of a launch; a launch's traffic grows with the sources it carries.
-    traffic_per_src = {"fwd64": 0.279e6, "adj64": 0.347e6}
-    traffic = traffic_per_src[dom] * len(srnum) if dom in traffic_per_src else None
+    # DRAM traffic per launch of the polish kernels: the algorithmic bytes per launch times the
+    # ratio of measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum over the
+    # 1680 launches of the phase, 9-source case of this grid) to the algorithmic bytes of the
+    # same launches.  The excess over 1 is the halo re-read.
+    traffic_ratio = {"fwd64": 1.14, "adj64": 1.89}
+    traffic = (alg_bytes / launches_dom * traffic_ratio[dom]) if (dom in traffic_ratio and launches_dom) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_unit": "bytes per launch",
+                "traffic_over_algorithmic": traffic_ratio.get(dom),
                 "algorithmic_bytes_per_launch": alg_bytes / launches_dom if launches_dom else None,
                 "kernel": kname, "phase": dom,
                 "peak_kind": peak_kind, "node_updates_per_s": upd_dom / (ms_dom / 1e3) if ms_dom > 0 else 0.0,
