@@ -82,6 +82,30 @@ __device__ __forceinline__ float narrow_trunc(double x) {
     if (mag >= (1151u << 20)) return __uint_as_float(sign | 0x7f7fffffu);
     return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
 }
+// (float)(v - r) for doubles v, r >= 0 without an FP64 instruction: each is split on the
+// integer pipe into h + l (h: its top 24 significant bits, l: the next 29 bits rounded down to
+// an FP32 value), and (h_v - h_r) + (l_v - l_r) is formed in FP32.  The heads' difference is
+// exact when v and r are within a factor 2 (Sterbenz), so the result has the difference's
+// FP32 precision although v and r are large (the FP32 kernels' traveltime offsets).
+__device__ __forceinline__ float2 split_hl(double x) {
+    const unsigned long long b = (unsigned long long)dbits(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned mag = hi & 0x7fffffffu;
+    if (mag < (897u << 20)) return make_float2(0.0f, 0.0f);   // below 2^-126: negligible here
+    const float h = __uint_as_float(((mag - (896u << 20)) << 3) | (lo >> 29));
+    const unsigned r = lo & 0x1fffffffu;
+    if (r == 0u) return make_float2(h, 0.0f);
+    const int n = __clz(r);   // r's leading one at bit 31 - n
+    const int e = (int)(mag >> 20) - 1023 - 52 + (31 - n);
+    if (e < -126) return make_float2(h, 0.0f);
+    const unsigned frac = (unsigned)(((unsigned long long)r << (n + 1)) & 0xffffffffull) >> 9;
+    return make_float2(h, __uint_as_float(((unsigned)(e + 127) << 23) | frac));
+}
+__device__ __forceinline__ float offset_f32(double v, double r) {
+    const float2 a = split_hl(v), c = split_hl(r);
+    return (a.x - c.x) + (a.y - c.y);
+}
+
 __device__ __forceinline__ double widen_exact(float f) {
     const unsigned u = __float_as_uint(f), mag = u & 0x7fffffffu;
     if (mag < 0x00800000u) return 0.0;

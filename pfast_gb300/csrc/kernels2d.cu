@@ -295,10 +295,12 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
         if constexpr (sizeof(Aux) == 8) {
             load_box2(tbox, T, i0, j0, nr, nc, Aux(0), lane, Ident2());
         } else {
+            // offsets from the tile corner's traveltime, formed without FP64 instructions
+            const long long inf = dbits(kInf);
             double tr = T[(long long)i0 * nc + j0];
-            if (tr >= kInf) tr = 0.0;
+            if (dbits(tr) >= inf) tr = 0.0;
             load_box2(tbox, T, i0, j0, nr, nc, Aux(0), lane,
-                      [tr](double v) { return v >= kInf ? (Aux)INFINITY : (Aux)(v - tr); });
+                      [tr, inf](double v) { return dbits(v) >= inf ? (Aux)INFINITY : (Aux)offset_f32(v, tr); });
         }
         if (lane_ok) {
             const unsigned* mrow = A.mask + A.mask_off[q] + (long long)gi * A.wpr + (j0 >> 5);
@@ -464,13 +466,17 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
         if (f_jhi && tj < A.nbj - 1) atomicOr(dirty + tid + 1, 0xf);
     }
     bool moved = false;
+    const float tabs_f = narrow_trunc(A.tol_abs), trel_f = narrow_trunc(A.tol_rel);   // FP32 kinds' test
     for (int y = 0; y < ei; ++y) {
         for (int x = lane; x < ej; x += 32) {
             const long long at = (long long)(i0 + y) * nc + j0 + x;
             const Real v = box[(y + 1) * R2 + x + 1];
             fld[at] = v;
-            const double diff = fabs((double)__ldcg(snp + at) - (double)v);
-            if (diff > A.tol_abs + A.tol_rel * fabs((double)v)) moved = true;
+            if constexpr (sizeof(Real) == 8) {
+                if (fabs(__ldcg(snp + at) - v) > A.tol_abs + A.tol_rel * fabs(v)) moved = true;   // isconv
+            } else {
+                if (fabsf(__ldcg(snp + at) - v) > tabs_f + trel_f * fabsf(v)) moved = true;
+            }
         }
     }
     const bool any_moved = __any_sync(0xffffffffu, moved);
