@@ -24,10 +24,18 @@ template <> struct Traits2<kAdjPlain64>  { using Real = double; using Aux = doub
 template <> struct Traits2<kAdjFast32>   { using Real = float;  using Aux = float;  static constexpr bool adj = true; };
 template <> struct Traits2<kAdjPolish64> { using Real = double; using Aux = double; static constexpr bool adj = true; };
 
+// The FP64 adjoint kinds read the traveltime through register windows (no second FP64 box);
+// the FP32 bulk adjoint stages it as a box of FP32 offsets.
+template <int KIND>
+__host__ __device__ constexpr bool t_windows2() {
+    return Traits2<KIND>::adj && sizeof(typename Traits2<KIND>::Aux) == 8;
+}
+
 template <int KIND>
 __host__ __device__ constexpr int warp_smem2() {
     using T = Traits2<KIND>;
-    return int(H2I * R2 * sizeof(typename T::Real) + (T::adj ? H2I * R2 * sizeof(typename T::Aux) : 0));
+    return int(H2I * R2 * sizeof(typename T::Real) +
+               (T::adj && !t_windows2<KIND>() ? H2I * R2 * sizeof(typename T::Aux) : 0));
 }
 
 __device__ __forceinline__ double ref_min(double x, double y) { return (x < y) ? x : y; }
@@ -292,9 +300,7 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     unsigned fixed_lo = 0, fixed_hi = 0;
     if constexpr (ADJ) {
         const double* T = reinterpret_cast<const double*>(A.aux) + A.aux_off[q];
-        if constexpr (sizeof(Aux) == 8) {
-            load_box2(tbox, T, i0, j0, nr, nc, Aux(0), lane, Ident2());
-        } else {
+        if constexpr (!t_windows2<KIND>()) {
             // offsets from the tile corner's traveltime, formed without FP64 instructions
             const long long inf = dbits(kInf);
             double tr = T[(long long)i0 * nc + j0];
@@ -338,9 +344,45 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     bool restep = false;   // polish: a remainder above the floor (visit again in this order)
     bool stale = false;    // FP32 bulk: a changed node feeds an in-tile node visited before it
 
+    // ---- adjoint traveltime of the FP64 kinds through register windows (as in the 3D sweeps):
+    // lane lif (flipped row) is at flipped column jf = t - lif in step t and keeps its row's
+    // traveltimes at jf-1, jf, jf+1 (loads issued three steps ahead); lane lif-1 is one column
+    // ahead and lane lif+1 one behind, so their windows hold the rows above and below at jf;
+    // lanes 0 and ei-1 read the halo rows outside the tile at their own position.
+    constexpr bool TWIN2 = t_windows2<KIND>();
+    const double* Tq = TWIN2 ? reinterpret_cast<const double*>(A.aux) + A.aux_off[q] : nullptr;
+    const int glo = i0 + (py ? -1 : ei), ghi = i0 + (py ? ei : -1);   // rows of flipped rows -1 and ei
+    const double* trow = (TWIN2 && lane_ok) ? Tq + (long long)gi * nc : nullptr;
+    const double* hlrow = (TWIN2 && lif == 0 && (unsigned)glo < (unsigned)nr) ? Tq + (long long)glo * nc : nullptr;
+    const double* hhrow =
+        (TWIN2 && lif == ei - 1 && (unsigned)ghi < (unsigned)nr) ? Tq + (long long)ghi * nc : nullptr;
+    auto tl = [&](const double* r, int p, int plo, int phi) -> double {
+        const int g = j0 + (px ? p : ej - 1 - p);
+        return (r != nullptr && p >= plo && p <= phi && (unsigned)g < (unsigned)nc) ? __ldg(r + g) : 0.0;
+    };
+    double tm = 0.0, t0w = 0.0, tp = 0.0, q1 = 0.0, q2 = 0.0;
+    double hl0 = 0.0, hl1 = 0.0, hl2 = 0.0, hh0 = 0.0, hh1 = 0.0, hh2 = 0.0;
+    if constexpr (TWIN2) {
+        const int f0 = -lif;
+        tm = tl(trow, f0 - 1, -1, ej); t0w = tl(trow, f0, -1, ej); tp = tl(trow, f0 + 1, -1, ej);
+        q1 = tl(trow, f0 + 2, -1, ej); q2 = tl(trow, f0 + 3, -1, ej);
+        hl0 = tl(hlrow, f0, 0, ej - 1); hl1 = tl(hlrow, f0 + 1, 0, ej - 1); hl2 = tl(hlrow, f0 + 2, 0, ej - 1);
+        hh0 = tl(hhrow, f0, 0, ej - 1); hh1 = tl(hhrow, f0 + 1, 0, ej - 1); hh2 = tl(hhrow, f0 + 2, 0, ej - 1);
+    }
+
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
         const int ljf = t - lif;
+        // adjoint: the traveltimes around this lane's node, in grid orientation
+        Aux T0 = Aux(0), Txm = Aux(0), Txp = Aux(0), Tzm = Aux(0), Tzp = Aux(0);
+        if constexpr (TWIN2) {
+            const double up = __shfl_sync(0xffffffffu, tm, (lane - 1) & 31);
+            const double dn = __shfl_sync(0xffffffffu, tp, (lane + 1) & 31);
+            const double fim = lif == 0 ? hl0 : up, fip = lif == ei - 1 ? hh0 : dn;
+            T0 = t0w;
+            Txm = px ? tm : tp; Txp = px ? tp : tm;
+            Tzm = py ? fim : fip; Tzp = py ? fip : fim;
+        }
         if (lane_ok && ljf >= 0 && ljf < ej) {
             const int lj = px ? ljf : ej - 1 - ljf;
             const int c = cb + lj;
@@ -394,21 +436,21 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                 if (row_interior && gj >= 1 && gj <= nc - 2 && !(fb & 1u)) {
                     const Real old = box[c];
                     Real r = old;
+                    if constexpr (!TWIN2) {   // FP32 bulk: from the staged offsets
+                        T0 = tbox[c]; Txp = tbox[c + 1]; Txm = tbox[c - 1]; Tzp = tbox[c + R2]; Tzm = tbox[c - R2];
+                    }
                     if constexpr (KIND == kAdjPlain64) {
-                        r = adj2_plain(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
-                                       box[c - 1], box[c + R2], box[c - R2], A.dx, A.dz);
+                        r = adj2_plain(T0, Txp, Txm, Tzp, Tzm, box[c + 1], box[c - 1], box[c + R2], box[c - R2], A.dx,
+                                       A.dz);
                     } else if constexpr (KIND == kAdjFast32) {
-                        r = adj2_bulk(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
-                                      box[c - 1], box[c + R2], box[c - R2], (float)A.inv2x, (float)A.inv2z);
+                        r = adj2_bulk(T0, Txp, Txm, Tzp, Tzm, box[c + 1], box[c - 1], box[c + R2], box[c - R2], wx, wz);
                     } else {
-                        const unsigned m = adj_orders2(dbits(tbox[c]), dbits(tbox[c - 1]), dbits(tbox[c + 1]),
-                                                       dbits(tbox[c - R2]), dbits(tbox[c + R2]));
+                        const unsigned m = adj_orders2(dbits(T0), dbits(Txm), dbits(Txp), dbits(Tzm), dbits(Tzp));
                         sel |= m;
                         if (m & obit) {
                             bool big = false;
-                            r = adj2_polish(tbox[c], tbox[c + 1], tbox[c - 1], tbox[c + R2], tbox[c - R2], box[c + 1],
-                                            box[c - 1], box[c + R2], box[c - R2], old, A.inv2x, A.inv2z, A.wxf,
-                                            A.wzf, A.polish_floor, big);
+                            r = adj2_polish(T0, Txp, Txm, Tzp, Tzm, box[c + 1], box[c - 1], box[c + R2], box[c - R2],
+                                            old, A.inv2x, A.inv2z, A.wxf, A.wzf, A.polish_floor, big);
                             restep |= big;
                         }
                     }
@@ -418,17 +460,17 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         if constexpr (kPrune) {
                             // lambda at the neighbour node reads this node if its traveltime is larger
                             // (FP32 bulk: offsets from the tile's corner, compared as values)
-                            auto dep = [&](int n) {
-                                if constexpr (sizeof(Aux) == 8) return obits2(tbox[c]) > obits2(tbox[n]);
-                                else return tbox[c] > tbox[n];
+                            auto dep = [&](Aux tn) {
+                                if constexpr (sizeof(Aux) == 8) return obits2(T0) > obits2(tn);
+                                else return T0 > tn;
                             };
-                            if (li == 0 && dep(c - R2)) m_ilo = true;
-                            if (li == ei - 1 && dep(c + R2)) m_ihi = true;
-                            if (lj == 0 && dep(c - 1)) chg_jlo = true;
-                            if (lj == ej - 1 && dep(c + 1)) chg_jhi = true;
+                            if (li == 0 && dep(Tzm)) m_ilo = true;
+                            if (li == ei - 1 && dep(Tzp)) m_ihi = true;
+                            if (lj == 0 && dep(Txm)) chg_jlo = true;
+                            if (lj == ej - 1 && dep(Txp)) chg_jhi = true;
                             if constexpr (!kSelective) {
-                                if (lif > 0 && dep(py ? c - R2 : c + R2)) stale = true;
-                                if (ljf > 0 && dep(px ? c - 1 : c + 1)) stale = true;
+                                if (lif > 0 && dep(py ? Tzm : Tzp)) stale = true;
+                                if (ljf > 0 && dep(px ? Txm : Txp)) stale = true;
                             }
                         } else {
                             if (lj == 0) chg_jlo = true;
@@ -437,6 +479,11 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                     }
                 }
             }
+        }
+        if constexpr (TWIN2) {   // slide the windows to step t + 1
+            tm = t0w; t0w = tp; tp = q1; q1 = q2; q2 = tl(trow, t + 4 - lif, -1, ej);
+            hl0 = hl1; hl1 = hl2; hl2 = tl(hlrow, t + 3 - lif, 0, ej - 1);
+            hh0 = hh1; hh1 = hh2; hh2 = tl(hhrow, t + 3 - lif, 0, ej - 1);
         }
         __syncwarp();
     }
