@@ -320,8 +320,10 @@ __device__ __forceinline__ long long obits(float x) { return __float_as_int(x); 
 // not depend on the order, so one quiet processing locks the tile for all eight; the
 // polish updates select nodes by sweep order (octant selection), so a tile locks for
 // an order only once it has been quiet in that order.  Per (source, tile):
-//   dirty[t]  bit o set: process the tile in sweep order o; all eight bits are set by
-//             the tile itself or a face neighbour when a node changes,
+//   dirty[t]  bit o set: process the tile in sweep order o; set at the start (all tiles,
+//             or for the FP32 bulk and the adjoint polish the tiles with something to
+//             propagate), and for all eight orders by a face neighbour whose changed face
+//             node the tile reads, or by the tile itself (see process_tile),
 //   stamp[t]  outer iteration in which the tile last took its snapshot,
 //   diff[t]   whether the tile differs from its snapshot by more than the
 //             tolerance after its latest processing (cleared each iteration).
@@ -338,8 +340,8 @@ __device__ __forceinline__ int tile_of(const Sweep3Args& A, unsigned pk, int dir
 }
 
 // Whether a tile with lock word dm is processed in sweep order dir.  Polish kinds: bits 8-15
-// hold the orders in which some node of the tile is selected (recorded at the tile's last
-// processing; all eight before the first).
+// hold the orders in which some node of the tile is selected (from the order pre-pass, then
+// recorded at each processing).
 template <int KIND>
 __device__ __forceinline__ bool tile_due(int dm, int dir) {
     constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
