@@ -119,6 +119,7 @@ SIGNATURES = [
     ("pfast_ctx_create", _i, [_i, _p]),
     ("pfast_ctx_destroy", _i, [_p]),
     ("pfast_ctx_set_stream", _i, [_p, _p]),
+    ("pfast_ctx_set_graphs", _i, [_p, C.c_int]),
     ("pfast_ctx_synchronize", _i, [_p]),
     ("pfast_fsm3d", _i, [_p, _p, _p, _i, _i, _d, _d, _d, _i, _i, _i, _i]),
     ("pfast_adjoint_fsm3d", _i, [_p, _p, _p, _p, _p, _p, _p, _i, _i, _d, _d, _d, _i, _i, _i, _i, _p]),

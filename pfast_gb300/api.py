@@ -115,6 +115,10 @@ class Context:
         """Run on a cudaStream_t (an int handle, e.g. torch.cuda.current_stream().cuda_stream); None = own stream."""
         check(lib().pfast_ctx_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None), "set_stream")
 
+    def set_graphs(self, enabled):
+        """Replay per-diagonal 3D outer iterations as CUDA graphs (default) or launch one by one."""
+        check(lib().pfast_ctx_set_graphs(self._h, 1 if enabled else 0), "set_graphs")
+
     def synchronize(self):
         check(lib().pfast_ctx_synchronize(self._h), "synchronize")
 

@@ -84,7 +84,7 @@ std::vector<DevBuf*> ctx_buffers(pfast_ctx* ctx) {
     return {&ctx->s64,  &ctx->s32,  &ctx->sq64,     &ctx->T32,    &ctx->tflags,    &ctx->T64,   &ctx->L64,
             &ctx->scratch, &ctx->mask, &ctx->act,  &ctx->changed, &ctx->ee,     &ctx->need,    &ctx->misc,
             &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a, &ctx->f2b, &ctx->f2c, &ctx->work,
-            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c};
+            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c, &ctx->dyn};
 }
 
 void ctx_release_buffers(pfast_ctx* ctx) {
@@ -93,7 +93,8 @@ void ctx_release_buffers(pfast_ctx* ctx) {
 
 void ctx_stream_ordered(pfast_ctx* ctx) {
     for (DevBuf* b : ctx_buffers(ctx)) b->astream = ctx->own_stream;
-    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work}) b->sstream = ctx->own_stream;
+    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work, &ctx->h_dyn})
+        b->sstream = ctx->own_stream;
 }
 
 void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc) {
@@ -183,6 +184,54 @@ static void tune_record(const std::tuple<int, int, int, int, int, int>& key, int
     e.n[which] += 1;
 }
 
+// One outer iteration of a per-diagonal phase as a CUDA graph: the diff reset, the 8 x ndiag
+// sweep launches and the per-instance reduction, captured once per (kind, launch arguments,
+// active count) and replayed every iteration -- one launch instead of 8 x ndiag + 1.  The
+// launches read the iteration and the current active count from ctx->dyn (a.dyn), written
+// before each replay; blocks of instances that retired since the capture exit at once.
+static pfast_status iteration_graph(pfast_ctx* ctx, const Sweep3Args& a, int kind, const DiagTable3& dt, int nb,
+                                    int nact, cudaStream_t st, cudaGraphExec_t* out) {
+    Sweep3Args k = a;
+    k.dir = 0;
+    k.iter = 0;
+    const int extra[4] = {kind, nact, nb, dt.ndiag};
+    std::vector<unsigned char> key(sizeof(k) + sizeof(extra));
+    std::memcpy(key.data(), &k, sizeof(k));
+    std::memcpy(key.data() + sizeof(k), extra, sizeof(extra));
+    for (auto& g : ctx->iter_graphs)
+        if (g.first == key) { *out = g.second; return PFAST_OK; }
+    cudaGraph_t graph = nullptr;
+    PFAST_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    pfast_status r = PFAST_OK;
+    cudaError_t e = cudaMemsetAsync(k.diff, 0, sizeof(int) * (size_t)k.ntiles * nb, st);
+    for (int dir = 0; dir < 8 && !r && e == cudaSuccess; ++dir) {
+        k.dir = dir;
+        for (int d = 0; d < dt.ndiag && !r; ++d) r = launch_sweep3(kind, k, d, dt.h_off[d + 1] - dt.h_off[d], nact, st);
+    }
+    if (!r && e == cudaSuccess) e = cudaMemsetAsync(k.changed, 0, sizeof(int) * nb, st);
+    if (!r && e == cudaSuccess)
+        r = launch_reduce_diff(k.diff, k.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 8, 0xff, k.ntiles, k.act,
+                               nact, k.changed, st, k.dyn);
+    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (r || e != cudaSuccess || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (r) return r;
+        return cuda_fail(e != cudaSuccess ? e : ec, "iteration graph capture", __FILE__, __LINE__);
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    if (ctx->iter_graphs.size() >= 16) {   // bounded cache: drop the oldest
+        cudaGraphExecDestroy(ctx->iter_graphs.front().second);
+        ctx->iter_graphs.erase(ctx->iter_graphs.begin());
+    }
+    ctx->iter_graphs.emplace_back(std::move(key), exec);
+    *out = exec;
+    return PFAST_OK;
+}
+
 pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable3& dt, int nb,
                          std::vector<int>& active, int maxiter, int* iters, long long nodes_per_sweep,
                          long long* node_updates, int* not_conv, double* ms_acc) {
@@ -257,21 +306,39 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
         active.swap(still);
     }
     int it = 0;
+    const bool graph = ctx->graphs && !persistent && maxiter > 0 && !active.empty();
+    cudaGraphExec_t exec = nullptr;
+    if (graph) {
+        PFAST_TRY(ctx->dyn.ensure(2 * sizeof(int)));
+        PFAST_TRY(ctx->h_dyn.ensure(2 * sizeof(int)));
+        a.dyn = ctx->dyn.as<int>();
+    }
     while (!persistent && !active.empty() && it < maxiter) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
-        PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles * nb, st));
-        a.iter = it;
-        for (int dir = 0; dir < 8; ++dir) {
-            a.dir = dir;
-            for (int d = 0; d < dt.ndiag; ++d) {
-                PFAST_LAUNCH(ctx, launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
+        if (graph) {
+            // captured with the first iteration's active count; later iterations only retire instances
+            if (!exec) PFAST_TRY(iteration_graph(ctx, a, kind, dt, nb, nact, st, &exec));
+            int* hd = ctx->h_dyn.as<int>();
+            hd[0] = it;
+            hd[1] = nact;
+            PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->dyn.p, hd, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+            PFAST_CUDA_TRY(cudaGraphLaunch(exec, st));
+            ctx->launches += 8LL * dt.ndiag + 1;
+        } else {
+            PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles * nb, st));
+            a.iter = it;
+            for (int dir = 0; dir < 8; ++dir) {
+                a.dir = dir;
+                for (int d = 0; d < dt.ndiag; ++d) {
+                    PFAST_LAUNCH(ctx, launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
+                }
             }
+            PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));
+            PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 8, 0xff,
+                                                 a.ntiles, a.act, nact, a.changed, st));
         }
-        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));
-        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 8, 0xff,
-                                             a.ntiles, a.act, nact, a.changed, st));
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) return cuda_fail(le, "sweep launch", __FILE__, __LINE__);
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
@@ -645,7 +712,8 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     pfast::ctx_release_buffers(ctx);
-    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work}) b->release();
+    for (HostBuf* b : {&ctx->h_act, &ctx->h_changed, &ctx->h_ee, &ctx->h_need, &ctx->h_work, &ctx->h_dyn}) b->release();
+    for (auto& g : ctx->iter_graphs) cudaGraphExecDestroy(g.second);
     for (auto& kv : ctx->diag3) free_diag_table3(kv.second);
     for (auto& kv : ctx->diag2) free_diag_table2(kv.second);
     for (auto& ev : ctx->ev)
@@ -658,6 +726,12 @@ pfast_status pfast_ctx_destroy(pfast_ctx* ctx) {
 pfast_status pfast_ctx_set_stream(pfast_ctx* ctx, void* stream) {
     if (!ctx) { set_last_error("null context"); return PFAST_ERR_INVALID; }
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return PFAST_OK;
+}
+
+pfast_status pfast_ctx_set_graphs(pfast_ctx* ctx, int enabled) {
+    if (!ctx) { set_last_error("null context"); return PFAST_ERR_INVALID; }
+    ctx->graphs = enabled != 0;
     return PFAST_OK;
 }
 

@@ -52,6 +52,12 @@ struct pfast_ctx {
     pfast::DevBuf work;                 // executed node updates per instance (sweep kernels)
     pfast::DevBuf queue;                // work counter of the persistent sweep kernel
     pfast::DevBuf out_a, out_b, out_c;  // request server: device outputs of a request
+    pfast::DevBuf dyn;                  // replayed iteration graphs: outer iteration, active instances
+    pfast::HostBuf h_dyn;
+    // One outer iteration of a per-diagonal phase as an instantiated CUDA graph, keyed by the
+    // sweep kind, the launch arguments and the active-instance count it was captured with.
+    std::vector<std::pair<std::vector<unsigned char>, cudaGraphExec_t>> iter_graphs;
+    bool graphs = true;                 // replay per-diagonal outer iterations as CUDA graphs
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
     std::map<std::pair<int, int>, pfast::DiagTable2> diag2;
     cudaEvent_t ev[8] = {};

@@ -42,6 +42,9 @@ struct Sweep3Args {
     float polish_floor;       // polish sweeps: corrections at or below this are dropped (seconds;
                               // adjoint: relative to 1 + |lambda|)
     unsigned long long* work; // per instance: nodes of the tiles processed (executed node updates); may be null
+    const int* dyn;           // per-diagonal launches of a replayed iteration graph: dyn[0] = outer
+                              // iteration (instead of iter), dyn[1] = active instances (blocks with
+                              // blockIdx.y >= dyn[1] exit); null: iter and the grid
 };
 
 // Tile-diagonal table for a grid: tiles (bk, bi, bj) in flipped coordinates with
@@ -61,7 +64,8 @@ size_t sweep3_smem_bytes(int kind);
 // tile still due in some order (lock words `dirty`: order bits order_mask, selected orders
 // `shift` bits higher for the selective polish kinds).
 pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selective, int shift, int order_mask,
-                                int ntiles, const int* act, int nact, int* changed, cudaStream_t st);
+                                int ntiles, const int* act, int nact, int* changed, cudaStream_t st,
+                                const int* dyn = nullptr);
 // Polish kinds: the tile's initially selected orders in bits 8-15 of its lock word (bits 0-7
 // kept: all orders due, or as seeded), computed from a.field (forward) or a.aux (adjoint) for
 // the active instances a.act[0..nact).

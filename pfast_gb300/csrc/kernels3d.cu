@@ -684,13 +684,18 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
     const int d0 = A.diag_off[d];
     const int tile_idx = blockIdx.x * kWarps3 + warp;
     if (tile_idx >= A.diag_off[d + 1] - d0) return;
+    int iter = A.iter;
+    if (A.dyn) {   // replayed iteration graph
+        if ((int)blockIdx.y >= __ldcg(A.dyn + 1)) return;
+        iter = __ldcg(A.dyn);
+    }
     const int inst = A.act[blockIdx.y];
     int tk, ti, tj;
     const int tid = tile_of(A, A.diag_tiles[d0 + tile_idx], A.dir, tk, ti, tj);
     const int dm = __ldcg(A.dirty + (long long)inst * A.ntiles + tid);
     if (!tile_due<KIND>(dm, A.dir)) return;   // locked tile for this order (warp-uniform)
     __syncwarp();
-    process_tile<KIND, false>(A, inst, tid, tk, ti, tj, A.dir, A.iter, dm, smem_raw + warp * warp_smem_bytes<KIND>(),
+    process_tile<KIND, false>(A, inst, tid, tk, ti, tj, A.dir, iter, dm, smem_raw + warp * warp_smem_bytes<KIND>(),
                               lane);
 }
 
@@ -850,7 +855,8 @@ __global__ void seed_tiles_kernel(const Sweep3Args A) {
 // hold the selected orders `shift` bits higher, and an order counts when due and selected).
 __global__ void reduce_diff_kernel(const int* __restrict__ diff, const int* __restrict__ dirty, int selective,
                                    int shift, int order_mask, int ntiles, const int* __restrict__ act,
-                                   int* __restrict__ changed) {
+                                   int* __restrict__ changed, const int* __restrict__ dyn) {
+    if (dyn && (int)blockIdx.x >= __ldcg(dyn + 1)) return;   // replayed graph: beyond the active count
     const int inst = act[blockIdx.x];
     const int* d = diff + (long long)inst * ntiles;
     const int* w = dirty + (long long)inst * ntiles;
@@ -1044,9 +1050,10 @@ pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int na
 }
 
 pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selective, int shift, int order_mask,
-                                int ntiles, const int* act, int nact, int* changed, cudaStream_t st) {
+                                int ntiles, const int* act, int nact, int* changed, cudaStream_t st, const int* dyn) {
     if (nact <= 0) return PFAST_OK;
-    reduce_diff_kernel<<<nact, 256, 0, st>>>(diff, dirty, selective ? 1 : 0, shift, order_mask, ntiles, act, changed);
+    reduce_diff_kernel<<<nact, 256, 0, st>>>(diff, dirty, selective ? 1 : 0, shift, order_mask, ntiles, act, changed,
+                                             dyn);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "reduce_diff launch", __FILE__, __LINE__);
     return PFAST_OK;

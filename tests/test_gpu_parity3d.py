@@ -300,3 +300,27 @@ def test_schedule_autotune(ctx):
     g_diag, e_diag, _ = sv.eval(d_vp, precision=pg.PFAST_MIXED, schedule=pg._capi.PFAST_SCHEDULE_DIAGONAL)
     assert bits_equal(g_auto.cpu().numpy(), g_diag.cpu().numpy()) and e_auto == e_diag
     sv.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_graph_replay_matches_launches(ctx, precision):
+    # per-diagonal outer iterations replayed as captured CUDA graphs give the bits (and the
+    # iteration counts) of launching the kernels one by one
+    pg, torch = _pg(), _torch()
+    prec = pg.PFAST_PLAIN_FP64 if precision == "plain" else pg.PFAST_MIXED
+    shape, h = (12, 18, 40), (20.0, 20.0, 20.0)
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 11)
+    sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src, srnum, rec, nxyz, tobs)
+    d = torch.from_numpy(vp).cuda()
+    try:
+        ctx.set_graphs(False)
+        g0, e0, s0 = sv.eval(d, precision=prec, schedule=1)
+        ctx.set_graphs(True)
+        g1, e1, s1 = sv.eval(d, precision=prec, schedule=1)
+        g2, e2, s2 = sv.eval(d, precision=prec, schedule=1)   # the cached graphs replayed
+    finally:
+        ctx.set_graphs(True)
+    assert bits_equal(g0.cpu().numpy(), g1.cpu().numpy()) and e0 == e1
+    assert bits_equal(g0.cpu().numpy(), g2.cpu().numpy()) and e0 == e2
+    for k in ("fwd_iters_max", "adj_iters_max", "fwd32_iters_max", "adj32_iters_max", "launches"):
+        assert s0[k] == s1[k] == s2[k], k
