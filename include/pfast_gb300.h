@@ -93,8 +93,8 @@ pfast_status pfast_ctx_create(int device, pfast_ctx** out);
 pfast_status pfast_ctx_destroy(pfast_ctx* ctx);
 /* Run subsequent work on `stream` (a cudaStream_t); NULL restores the context's own stream. */
 pfast_status pfast_ctx_set_stream(pfast_ctx* ctx, void* stream);
-/* Per-diagonal 3D sweeps: replay each outer iteration as a captured CUDA graph (enabled = 1,
-   the default) or launch its kernels one by one (0; results are the same). */
+/* Per-diagonal sweeps (3D and 2D): replay each outer iteration as a captured CUDA graph
+   (enabled = 1, the default) or launch its kernels one by one (0; results are the same). */
 pfast_status pfast_ctx_set_graphs(pfast_ctx* ctx, int enabled);
 pfast_status pfast_ctx_synchronize(pfast_ctx* ctx);
 

@@ -116,7 +116,7 @@ class Context:
         check(lib().pfast_ctx_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None), "set_stream")
 
     def set_graphs(self, enabled):
-        """Replay per-diagonal 3D outer iterations as CUDA graphs (default) or launch one by one."""
+        """Replay per-diagonal outer iterations (3D and 2D) as CUDA graphs (default) or launch one by one."""
         check(lib().pfast_ctx_set_graphs(self._h, 1 if enabled else 0), "set_graphs")
 
     def synchronize(self):

@@ -74,6 +74,52 @@ pfast_status upload_inst(pfast_ctx* ctx, DevBuf& buf, const InstTables& t, InstD
     return PFAST_OK;
 }
 
+// One outer iteration of a 2D phase as a replayed CUDA graph (see the 3D sweeps): the diff
+// reset, the 4 x ndiag launches and the per-instance reduction, captured once per (kind,
+// arguments, active count); the launches read the iteration and the active count from a.dyn.
+static pfast_status iteration_graph2(pfast_ctx* ctx, const Sweep2Args& a, int kind, const DiagTable2& dt, int ninst,
+                                     int nact, cudaStream_t st, cudaGraphExec_t* out) {
+    Sweep2Args k = a;
+    k.dir = 0;
+    k.iter = 0;
+    const int extra[5] = {2, kind, nact, ninst, dt.ndiag};
+    std::vector<unsigned char> key(sizeof(k) + sizeof(extra));
+    std::memcpy(key.data(), &k, sizeof(k));
+    std::memcpy(key.data() + sizeof(k), extra, sizeof(extra));
+    for (auto& g : ctx->iter_graphs)
+        if (g.first == key) { *out = g.second; return PFAST_OK; }
+    cudaGraph_t graph = nullptr;
+    PFAST_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    pfast_status r = PFAST_OK;
+    cudaError_t e = cudaMemsetAsync(k.diff, 0, sizeof(int) * (size_t)k.ntiles * ninst, st);
+    for (int dir = 0; dir < 4 && !r && e == cudaSuccess; ++dir) {
+        k.dir = dir;
+        for (int d = 0; d < dt.ndiag && !r; ++d) r = launch_sweep2(kind, k, d, dt.h_off[d + 1] - dt.h_off[d], nact, st);
+    }
+    if (!r && e == cudaSuccess) e = cudaMemsetAsync(k.changed, 0, sizeof(int) * ninst, st);
+    if (!r && e == cudaSuccess)
+        r = launch_reduce_diff(k.diff, k.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 4, 0xf, k.ntiles, k.act,
+                               nact, k.changed, st, k.dyn);
+    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (r || e != cudaSuccess || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (r) return r;
+        return cuda_fail(e != cudaSuccess ? e : ec, "iteration graph capture", __FILE__, __LINE__);
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    if (ctx->iter_graphs.size() >= 16) {   // bounded cache: drop the oldest
+        cudaGraphExecDestroy(ctx->iter_graphs.front().second);
+        ctx->iter_graphs.erase(ctx->iter_graphs.begin());
+    }
+    ctx->iter_graphs.emplace_back(std::move(key), exec);
+    *out = exec;
+    return PFAST_OK;
+}
+
 // Outer iterations of a 2D phase; caps[q] = iteration cap of instance q.
 pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable2& dt, int ninst,
                          std::vector<int>& active, const std::vector<int>& caps, int* iters, long long nodes,
@@ -120,21 +166,39 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
     a.work = ctx->work.as<unsigned long long>();
     PFAST_CUDA_TRY(cudaMemsetAsync(a.work, 0, sizeof(unsigned long long) * ninst, st));
     int it = 0;
+    const bool graph = ctx->graphs && !active.empty();
+    cudaGraphExec_t exec = nullptr;
+    if (graph) {
+        PFAST_TRY2(ctx->dyn.ensure(2 * sizeof(int)));
+        PFAST_TRY2(ctx->h_dyn.ensure(2 * sizeof(int)));
+        a.dyn = ctx->dyn.as<int>();
+    }
     while (!active.empty()) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
-        PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles * ninst, st));
-        a.iter = it;
-        for (int dir = 0; dir < 4; ++dir) {
-            a.dir = dir;
-            for (int d = 0; d < dt.ndiag; ++d) {
-                PFAST_LAUNCH(ctx, launch_sweep2(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
+        if (graph) {
+            // captured with the first iteration's active count; later iterations only retire instances
+            if (!exec) PFAST_TRY2(iteration_graph2(ctx, a, kind, dt, ninst, nact, st, &exec));
+            int* hd = ctx->h_dyn.as<int>();
+            hd[0] = it;
+            hd[1] = nact;
+            PFAST_CUDA_TRY(cudaMemcpyAsync(ctx->dyn.p, hd, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+            PFAST_CUDA_TRY(cudaGraphLaunch(exec, st));
+            ctx->launches += 4LL * dt.ndiag + 1;
+        } else {
+            PFAST_CUDA_TRY(cudaMemsetAsync(a.diff, 0, sizeof(int) * ntiles * ninst, st));
+            a.iter = it;
+            for (int dir = 0; dir < 4; ++dir) {
+                a.dir = dir;
+                for (int d = 0; d < dt.ndiag; ++d) {
+                    PFAST_LAUNCH(ctx, launch_sweep2(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
+                }
             }
+            PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * ninst, st));
+            PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 4, 0xf,
+                                                 a.ntiles, a.act, nact, a.changed, st));
         }
-        PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * ninst, st));
-        PFAST_LAUNCH(ctx, launch_reduce_diff(a.diff, a.dirty, kind == kFwdPolish64 || kind == kAdjPolish64, 4, 0xf,
-                                             a.ntiles, a.act, nact, a.changed, st));
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) return cuda_fail(le, "sweep2 launch", __FILE__, __LINE__);
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * ninst, cudaMemcpyDeviceToHost, st));

@@ -259,6 +259,11 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     const int d0 = A.diag_off[d];
     const int tile_idx = blockIdx.x * kWarps2 + warp;
     if (tile_idx >= A.diag_off[d + 1] - d0) return;
+    int iter = A.iter;
+    if (A.dyn) {   // replayed iteration graph
+        if ((int)blockIdx.y >= __ldcg(A.dyn + 1)) return;
+        iter = __ldcg(A.dyn);
+    }
     const int q = A.act[blockIdx.y];
 
     const unsigned pk = A.diag_tiles[d0 + tile_idx];
@@ -317,10 +322,10 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
 
     // snapshot at the tile's first processing in this outer iteration
     int* stamp = A.stamp + (long long)q * A.ntiles;
-    if (__ldcg(stamp + tid) != A.iter) {
+    if (__ldcg(stamp + tid) != iter) {
         for (int y = 0; y < ei; ++y)
             for (int x = lane; x < ej; x += 32) snp[(long long)(i0 + y) * nc + j0 + x] = box[(y + 1) * R2 + x + 1];
-        if (lane == 0) stamp[tid] = A.iter;
+        if (lane == 0) stamp[tid] = iter;
     }
     __syncwarp();
 

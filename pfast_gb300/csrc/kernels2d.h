@@ -42,6 +42,8 @@ struct Sweep2Args {
     int* diff;                   // per (instance, tile): moved beyond the tolerance this iteration
     unsigned long long* work;    // per instance: nodes of the tiles processed; may be null
     double tol_abs, tol_rel;
+    const int* dyn;              // replayed iteration graph: dyn[0] = outer iteration (instead of
+                                 // iter), dyn[1] = active instances; null: iter and the grid
 };
 
 struct DiagTable2 {

@@ -148,3 +148,29 @@ def test_reflector_without_node_above_is_an_error(ctx):
     with pytest.raises(pg.PfastError) as e:
         sv.forward(torch.full((nr, nc), 2000.0, dtype=torch.float64, device="cuda"))
     assert e.value.status == 5   # PFAST_ERR_NO_REFLECTION_POINT
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_graph_replay_matches_launches_2d(ctx, precision):
+    # 2D outer iterations replayed as captured CUDA graphs give the bits and iteration counts of
+    # launching the kernels one by one (joint transmission + reflection gradient)
+    pg, torch = _pg(), _torch()
+    prec = pg.PFAST_PLAIN_FP64 if precision == "plain" else pg.PFAST_MIXED
+    g = load_inv()
+    Z = load_fw()["Z"]
+    sv = pg.Survey2D(ctx, 160, 600, float(g["dx"]), float(g["dz"]), g["src"], g["srnum"], g["rec"].astype(np.int32),
+                     numofr=int(g["numofr"]), Z=Z, nxy=g["nxy"], tt_obs=g["tt"], tr_obs=g["tr"])
+    WR = torch.full((160, 600), float(g["wr"]), dtype=torch.float64, device="cuda")
+    vp = torch.from_numpy(g["vp"]).cuda()
+    try:
+        ctx.set_graphs(False)
+        r0 = sv.eval(vp, WR, precision=prec)
+        ctx.set_graphs(True)
+        r1 = sv.eval(vp, WR, precision=prec)
+    finally:
+        ctx.set_graphs(True)
+    for k in ("gT", "gR", "gRT"):
+        assert bits_equal(r0[k].cpu().numpy(), r1[k].cpu().numpy()), k
+    assert r0["Et"] == r1["Et"] and r0["Er"] == r1["Er"]
+    for k in ("fwd_iters_max", "adj_iters_max", "launches"):
+        assert r0["stats"][k] == r1["stats"][k], k
