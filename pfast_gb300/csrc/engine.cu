@@ -200,6 +200,14 @@ static pfast_status iteration_graph(pfast_ctx* ctx, const Sweep3Args& a, int kin
     std::memcpy(key.data() + sizeof(k), extra, sizeof(extra));
     for (auto& g : ctx->iter_graphs)
         if (g.first == key) { *out = g.second; return PFAST_OK; }
+    *out = nullptr;
+    bool seen = false;
+    for (auto& k2 : ctx->graph_seen) seen = seen || k2 == key;
+    if (!seen) {   // first occurrence: launch one by one this time
+        if (ctx->graph_seen.size() >= 64) ctx->graph_seen.erase(ctx->graph_seen.begin());
+        ctx->graph_seen.push_back(key);
+        return PFAST_OK;
+    }
     cudaGraph_t graph = nullptr;
     PFAST_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     pfast_status r = PFAST_OK;
@@ -306,20 +314,20 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
         active.swap(still);
     }
     int it = 0;
-    const bool graph = ctx->graphs && !persistent && maxiter > 0 && !active.empty();
     cudaGraphExec_t exec = nullptr;
-    if (graph) {
+    if (ctx->graphs && !persistent && maxiter > 0 && !active.empty()) {
+        // captured with the first iteration's active count; later iterations only retire instances
         PFAST_TRY(ctx->dyn.ensure(2 * sizeof(int)));
         PFAST_TRY(ctx->h_dyn.ensure(2 * sizeof(int)));
         a.dyn = ctx->dyn.as<int>();
+        PFAST_TRY(iteration_graph(ctx, a, kind, dt, nb, (int)active.size(), st, &exec));
+        if (!exec) a.dyn = nullptr;   // launched one by one
     }
     while (!persistent && !active.empty() && it < maxiter) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
-        if (graph) {
-            // captured with the first iteration's active count; later iterations only retire instances
-            if (!exec) PFAST_TRY(iteration_graph(ctx, a, kind, dt, nb, nact, st, &exec));
+        if (exec) {
             int* hd = ctx->h_dyn.as<int>();
             hd[0] = it;
             hd[1] = nact;

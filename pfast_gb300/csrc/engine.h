@@ -57,6 +57,9 @@ struct pfast_ctx {
     // One outer iteration of a per-diagonal phase as an instantiated CUDA graph, keyed by the
     // sweep kind, the launch arguments and the active-instance count it was captured with.
     std::vector<std::pair<std::vector<unsigned char>, cudaGraphExec_t>> iter_graphs;
+    // keys seen once: a phase is captured the second time its key comes up, so one-off shapes
+    // (uneven batches, a serving mix) do not pay for a graph they never replay
+    std::vector<std::vector<unsigned char>> graph_seen;
     bool graphs = true;                 // replay per-diagonal outer iterations as CUDA graphs
     std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
     std::map<std::pair<int, int>, pfast::DiagTable2> diag2;

@@ -316,8 +316,8 @@ def test_graph_replay_matches_launches(ctx, precision):
         ctx.set_graphs(False)
         g0, e0, s0 = sv.eval(d, precision=prec, schedule=1)
         ctx.set_graphs(True)
-        g1, e1, s1 = sv.eval(d, precision=prec, schedule=1)
-        g2, e2, s2 = sv.eval(d, precision=prec, schedule=1)   # the cached graphs replayed
+        g1, e1, s1 = sv.eval(d, precision=prec, schedule=1)   # phases captured the second time
+        g2, e2, s2 = sv.eval(d, precision=prec, schedule=1)   # their shapes come up, then replayed
     finally:
         ctx.set_graphs(True)
     assert bits_equal(g0.cpu().numpy(), g1.cpu().numpy()) and e0 == e1
