@@ -314,7 +314,7 @@ def main():
     ms_dom, upd_dom, w, kname = phases[dom]
     # FP64 instructions per executed node update of the polish kernels (the residual-form
     # updates; everything else in them runs on the integer and FP32 pipes)
-    fp64_per_update = {"fwd32": 0, "fwd64": 8, "adj32": 0, "adj64": 13}[dom]
+    fp64_per_update = {"fwd32": 0, "fwd64": 7, "adj32": 0, "adj64": 13}[dom]   # isotropic grid
     alg_bytes = upd_dom * 3 * w                       # read U + read slowness/T + write U per node update
     # launches of that kernel per evaluation: outer iterations x 8 sweep orders x tile diagonals
     # (4 x 8 x 32 tiles: nbk + nbi + nbj - 2 diagonals)

@@ -395,7 +395,7 @@ Sweep3Args base_args(const pfast_survey3d* sv) {
 
 }  // namespace
 
-pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed) {
+pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed, double sq_scale) {
     PFAST_TRY(ctx->s64.ensure(sizeof(double) * N));
     if (mixed) {
         PFAST_TRY(ctx->s32.ensure(sizeof(float) * N));
@@ -404,7 +404,8 @@ pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, boo
     PFAST_TRY(ctx->need.ensure(sizeof(int) * 4));
     PFAST_CUDA_TRY(cudaMemsetAsync(ctx->need.p, 0, sizeof(int), ctx->stream));
     PFAST_LAUNCH(ctx, launch_slowness(vp, ctx->s64.as<double>(), mixed ? ctx->s32.as<float>() : nullptr,
-                                      mixed ? ctx->sq64.as<double>() : nullptr, ctx->need.as<int>(), N, ctx->stream));
+                                      mixed ? ctx->sq64.as<double>() : nullptr, sq_scale, ctx->need.as<int>(), N,
+                                      ctx->stream));
     int bad = 0;
     PFAST_CUDA_TRY(cudaMemcpyAsync(&bad, ctx->need.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     PFAST_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -856,7 +857,9 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     cudaEvent_t t0 = ctx->ev[6], t1 = ctx->ev[7];
     PFAST_CUDA_TRY(cudaEventRecord(t0, s));
     const long long launches0 = ctx->launches;
-    PFAST_TRY(prepare_slowness(ctx, vp, N, o.precision == PFAST_MIXED));
+    // the 3D forward polish on an isotropic grid works with (s h)^2 (its residual divided by 1/h^2)
+    const double hsq = (sv->dx == sv->dy && sv->dy == sv->dz) ? sv->dx * sv->dx : 1.0;
+    PFAST_TRY(prepare_slowness(ctx, vp, N, o.precision == PFAST_MIXED, hsq));
     if (want_grad) PFAST_CUDA_TRY(cudaMemsetAsync(grad, 0, sizeof(double) * N, s));
     const size_t per_src = (size_t)N * (want_grad ? 24 : 16) + (size_t)sv->nz * sv->nr * ((sv->nc + 31) / 32) * 4;
     const int B = pick_batch(std::max(sv->nsrc, 1), o.max_batch, per_src);

@@ -154,9 +154,9 @@ pfast_status ctx_diag2(pfast_ctx* ctx, int nr, int nc, DiagTable2** out);
 // The process-wide context of the calling thread's current device (reference shims).
 pfast_status default_context(pfast_ctx** out);
 
-// Slowness arrays of a model (s64 always; s32 and s^2 for the mixed mode); rejects a
+// Slowness arrays of a model (s64 always; s32 and s^2 * sq_scale for the mixed mode); rejects a
 // model with a non-positive or non-finite velocity.
-pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed);
+pfast_status prepare_slowness(pfast_ctx* ctx, const double* vp, long long N, bool mixed, double sq_scale = 1.0);
 
 // Every device buffer of a context; release them all (stream-ordered for server contexts);
 // make a context's buffers stream-ordered on its own stream (request server slots).

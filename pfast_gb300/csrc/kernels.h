@@ -13,7 +13,7 @@ struct Sweep3Args {
     void* field;              // Real fields, per instance
     long long fstride;        // elements between instances (same for snap / aux / T)
     const void* aux;          // plain forward: slowness 1/vp (double); FP32 forward: slowness (float);
-                              // polish forward: slowness squared (double); adjoint: T per instance
+                              // polish forward: slowness squared, times h^2 on isotropic grids (double); adjoint: T per instance
                               // (double, or float for the FP32 adjoint)
     const double* slow64;     // polish forward: slowness (double), for the restart branch
     const unsigned* mask;     // adjoint: fixed-node bits, per instance, mask_stride words apart
@@ -85,9 +85,9 @@ pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, i
 pfast_status persistent_shape(int kind, int nact, int* warps, int* blocks);
 
 // Small 3D kernels.
-// s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64 (if non-null); *bad is set
+// s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64*sq_scale (if non-null); *bad is set
 // when some vp is not a positive finite number.
-pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, int* bad, long long n,
+pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, double sq_scale, int* bad, long long n,
                              cudaStream_t st);
 // Opt-in near-source start: nodes within `radius` nodes (Euclidean) of each instance's source get
 // 0.5*(s_src + s_node)*distance.  field: FP32 (is_fp32) or FP64 fields, fstride apart.

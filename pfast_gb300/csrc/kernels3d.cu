@@ -123,22 +123,29 @@ __device__ __forceinline__ float eik3_fast(float a, float b, float c, float s, c
 // floor, so the node wants another Newton step in the same order.
 __device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s2, const double* slow,
                                               long long node, const Spacing3& sp, float floor, bool& big) {
-    // FP64 for what fixes the root (the differences and the residual f, 8 FP64 instructions
-    // in the isotropic case); the derivative f' and the step in FP32.
+    // FP64 for what fixes the root (the differences and the residual f, 7 FP64 instructions
+    // in the isotropic case); the derivative f' and the step in FP32.  Isotropic grids: s2 holds
+    // (s h)^2 and f is the residual divided by 1/h^2 (same root, unit weights).
     const double px = pos_sign(U0 - a), py = pos_sign(U0 - b), pz = pos_sign(U0 - c);
     double f;
-    if (sp.iso) f = fma(sp.inv2[0], fma(px, px, fma(py, py, pz * pz)), -s2);
-    else f = fma(sp.inv2[0] * px, px, fma(sp.inv2[1] * py, py, fma(sp.inv2[2] * pz, pz, -s2)));
+    float wx, wy, wz;
+    if (sp.iso) {
+        f = fma(px, px, fma(py, py, fma(pz, pz, -s2)));
+        wx = wy = wz = 1.0f;
+    } else {
+        f = fma(sp.inv2[0] * px, px, fma(sp.inv2[1] * py, py, fma(sp.inv2[2] * pz, pz, -s2)));
+        wx = sp.wf[0]; wy = sp.wf[1]; wz = sp.wf[2];
+    }
     const float fx = narrow_trunc(px), fy = narrow_trunc(py), fz = narrow_trunc(pz);
-    const float fp = 2.0f * (sp.wf[0] * fx + sp.wf[1] * fy + sp.wf[2] * fz);
+    const float fp = 2.0f * (wx * fx + wy * fy + wz * fz);
     if (!(fp > 0.0f)) {
         big = true;
         const double s = __ldg(slow + node);
         return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
     }
     const float step = __fdividef(narrow_trunc(f), fp);
-    const float sw = (dbits(px) > 0 ? sp.wf[0] : 0.0f) + (dbits(py) > 0 ? sp.wf[1] : 0.0f) +
-                     (dbits(pz) > 0 ? sp.wf[2] : 0.0f);   // p >= 0: integer tests keep the FP64 pipe free
+    const float sw = (dbits(px) > 0 ? wx : 0.0f) + (dbits(py) > 0 ? wy : 0.0f) +
+                     (dbits(pz) > 0 ? wz : 0.0f);   // p >= 0: integer tests keep the FP64 pipe free
     big = sw * step * step > floor * fp;
     // corrections far below the 1e-9 convergence tolerance are dropped, so that a
     // converged region reaches a bitwise fixed point (and its tiles lock)
@@ -525,7 +532,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                         const float yb = ref_min(box[c - HJ], box[c + HJ]);
                         const float zc = ref_min(box[c - PS], box[c + PS]);
                         nv = ref_min(old, eik3_fast(xa, yb, zc, s, A.sp));
-                    } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2)
+                    } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2, (s h)^2 when isotropic)
                         // Octant selection: if an axis is active (U0 above its smaller neighbour) and
                         // that neighbour is the one this sweep visits after the node, the update would
                         // read a value the sweep has not refreshed; the node keeps its value and is
@@ -1084,14 +1091,14 @@ inline unsigned grid_for(long long n) {
 }
 
 __global__ void slowness_kernel(const double* __restrict__ vp, double* __restrict__ s64, float* __restrict__ s32,
-                                double* __restrict__ sq64, int* __restrict__ bad, long long n) {
+                                double* __restrict__ sq64, int* __restrict__ bad, long long n, double sq_scale) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         const double v = vp[t];
         if (!(v > 0.0 && v < INFINITY)) *bad = 1;
         const double s = 1.0 / v;   // s = 1.0/vp, src/T_pfsm3d.h:75
         s64[t] = s;
         if (s32) s32[t] = (float)s;
-        if (sq64) sq64[t] = s * s;
+        if (sq64) sq64[t] = (s * s) * sq_scale;
     }
 }
 
@@ -1248,9 +1255,9 @@ __global__ void gather3_kernel(const double* __restrict__ T, long long fstride, 
         if (e__ != cudaSuccess) return cuda_fail(e__, "kernel launch", __FILE__, __LINE__);    \
     } while (0)
 
-pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, int* bad, long long n,
+pfast_status launch_slowness(const double* vp, double* s64, float* s32, double* sq64, double sq_scale, int* bad, long long n,
                              cudaStream_t st) {
-    slowness_kernel<<<grid_for(n), kThreads, 0, st>>>(vp, s64, s32, sq64, bad, n);
+    slowness_kernel<<<grid_for(n), kThreads, 0, st>>>(vp, s64, s32, sq64, bad, n, sq_scale);
     PFAST_LAUNCH_CHECK();
     return PFAST_OK;
 }

@@ -144,7 +144,7 @@ extern "C" pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src
     PFAST_CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(unsigned) * tiles.size(), cudaMemcpyHostToDevice, s));
     PFAST_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, s));
 
-    pfast_status r = launch_slowness(vp, slow, nullptr, nullptr, d_bad, N, s);
+    pfast_status r = launch_slowness(vp, slow, nullptr, nullptr, 1.0, d_bad, N, s);
     if (r) return r;
     int bad = 0;
     PFAST_CUDA_TRY(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
