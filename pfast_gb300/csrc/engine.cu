@@ -271,13 +271,13 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     a.work = ctx->work.as<unsigned long long>();
     PFAST_CUDA_TRY(cudaMemsetAsync(a.work, 0, sizeof(unsigned long long) * nb, st));
     PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * nb, st));
-    const bool seeded = kind == kFwdFast32 || kind == kAdjFast32 || kind == kAdjPolish64;
+    const bool seeded = kind != kFwdPolish64;   // the forward polish starts from a reached field
     const bool polish = kind == kFwdPolish64 || kind == kAdjPolish64;
     if ((seeded || polish) && !active.empty()) {
         const int nact0 = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact0);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact0, cudaMemcpyHostToDevice, st));
-        // only tiles with something to propagate start due (the plain kinds start all due)
+        // only tiles with something to propagate start due
         if (seeded) PFAST_LAUNCH(ctx, launch_seed_tiles3(kind, a, nact0, st));
         // initial selected orders per tile, so the first polish sweep skips unselected tiles
         if (polish) PFAST_LAUNCH(ctx, launch_polish_orders3(kind, a, nb, nact0, st));

@@ -162,8 +162,8 @@ pfast_status run_sweeps2(pfast_ctx* ctx, Sweep2Args a, int kind, const DiagTable
     a.diff = a.stamp + ntiles * ninst;
     PFAST_CUDA_TRY(cudaMemsetAsync(a.dirty, 0xff, sizeof(int) * ntiles * ninst, st));
     PFAST_CUDA_TRY(cudaMemsetAsync(a.stamp, 0xff, sizeof(int) * ntiles * ninst, st));
-    if ((kind == kFwdFast32 || kind == kAdjFast32 || kind == kAdjPolish64) && !active.empty()) {
-        // only tiles with something to propagate start due (the plain kinds start all due)
+    if (kind != kFwdPolish64 && !active.empty()) {
+        // only tiles with something to propagate start due
         const int nact0 = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact0);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact0, cudaMemcpyHostToDevice, st));

@@ -70,9 +70,9 @@ pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selectiv
 // kept: all orders due, or as seeded), computed from a.field (forward) or a.aux (adjoint) for
 // the active instances a.act[0..nact).
 pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int nact, cudaStream_t st);
-// Initial lock words of the FP32 bulk kinds and the adjoint polish from the starting field
-// (a.field, active instances a.act[0..nact)): 0xff where the tile's halo box holds a reached
-// traveltime / nonzero lambda, else 0.  Other kinds: no-op.
+// Initial lock words from the starting field (a.field, active instances a.act[0..nact)): 0xff
+// where the tile's halo box holds a reached traveltime / nonzero lambda, else 0.  Every kind but
+// the forward polish (whose starting field is reached everywhere): no-op for that one.
 pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStream_t st);
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st);
 // Persistent sweep kernel: `blocks` blocks of `warps` warps take the nact instances of a.act

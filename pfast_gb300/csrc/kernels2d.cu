@@ -773,6 +773,8 @@ pfast_status launch_seed_tiles2(int kind, const Sweep2Args& a, int nact, cudaStr
     if (nact <= 0) return PFAST_OK;
     dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
     switch (kind) {
+        case kFwdPlain64: seed_tiles2_kernel<double, false, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjPlain64: seed_tiles2_kernel<double, true, false><<<grid, 256, 0, st>>>(a); break;
         case kFwdFast32: seed_tiles2_kernel<float, false, false><<<grid, 256, 0, st>>>(a); break;
         case kAdjFast32: seed_tiles2_kernel<float, true, false><<<grid, 256, 0, st>>>(a); break;
         case kAdjPolish64: seed_tiles2_kernel<double, true, true><<<grid, 256, 0, st>>>(a); break;

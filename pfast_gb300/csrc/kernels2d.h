@@ -56,9 +56,8 @@ struct DiagTable2 {
 pfast_status build_diag_table2(int nr, int nc, DiagTable2& t);
 void free_diag_table2(DiagTable2& t);
 pfast_status launch_sweep2(int kind, const Sweep2Args& a, int d, int tiles, int nact, cudaStream_t st);
-// Initial lock words of the FP32 bulk kinds and the adjoint polish from the starting field
-// (active instances a.act[0..nact)): due where the tile's halo box holds a reached traveltime /
-// nonzero lambda.  Other kinds: no-op.
+// Initial lock words from the starting field (active instances a.act[0..nact)): due where the
+// tile's halo box holds a reached traveltime / nonzero lambda.  The forward polish: no-op.
 pfast_status launch_seed_tiles2(int kind, const Sweep2Args& a, int nact, cudaStream_t st);
 
 // Init: field(q) = 0 at inst_src node (or (si,sj) from src_ij for q), INF elsewhere.

@@ -826,8 +826,11 @@ __global__ void tile_orders_kernel(const Sweep3Args A) {
 // (0xff) only if its halo box holds a value an update can propagate -- forward: a reached
 // traveltime (below the reference's INF); adjoint: a nonzero lambda -- and locked (0)
 // otherwise.  An update whose neighbours and own value are all unreached (all zero) returns
-// the same value, so such a tile is a fixed point until a neighbour's change marks it.  One
-// warp per tile, lane = column of the box rows.
+// the same value, so such a tile is a fixed point until a neighbour's change marks it.  That
+// holds bit for bit for the reference's updates too: every forward candidate from unreached
+// neighbours is at least INF, which the reference's MIN does not take over INF, and the
+// adjoint's POS/NEG terms of zero lambdas are +0 or -0, whose difference is +0.  One warp per
+// tile, lane = column of the box rows.
 template <typename Real, bool ADJ>
 __global__ void seed_tiles_kernel(const Sweep3Args A) {
     const int tid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -1036,6 +1039,8 @@ pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStr
     if (nact <= 0) return PFAST_OK;
     dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
     switch (kind) {
+        case kFwdPlain64: seed_tiles_kernel<double, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjPlain64: seed_tiles_kernel<double, true><<<grid, 256, 0, st>>>(a); break;
         case kFwdFast32: seed_tiles_kernel<float, false><<<grid, 256, 0, st>>>(a); break;
         case kAdjFast32: seed_tiles_kernel<float, true><<<grid, 256, 0, st>>>(a); break;
         case kAdjPolish64: seed_tiles_kernel<double, true><<<grid, 256, 0, st>>>(a); break;
