@@ -222,10 +222,12 @@ struct Ident2 {
 // Initial lock words from the field a phase starts from (as in the 3D sweeps): a tile is due
 // in every order only if its halo box holds a reached traveltime (forward) or a nonzero lambda
 // (adjoint); otherwise it is a fixed point of the update until a neighbour's change marks it.
-// SEL (polish): an idle tile keeps all four orders selected (bits 4-7), so that a neighbour's
-// mark makes it due.  One warp per tile, lane = column of the box rows.
+// SEL (the adjoint polish): an idle tile keeps all four orders selected (bits 4-7), so that a
+// neighbour's mark makes it due, and a tile counts as live only where some |lambda| exceeds a
+// quarter of the polish floor (smaller values give corrections within the floor).  One warp per tile, lane = column of the box rows.
 template <typename Real, bool ADJ, bool SEL>
 __global__ void seed_tiles2_kernel(const Sweep2Args A) {
+    const double thr = 0.25 * (double)A.polish_floor;   // SEL (adjoint polish): |lambda| above it
     const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (t >= A.ntiles) return;   // whole warps
     const int q = A.act[blockIdx.y];
@@ -241,7 +243,8 @@ __global__ void seed_tiles2_kernel(const Sweep2Args A) {
         for (int j = j0 - 1 + lane; j <= j0 + T2J; j += 32) {
             if ((unsigned)j >= (unsigned)nc) continue;
             const Real x = __ldg(f + (long long)i * nc + j);
-            v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
+            if constexpr (ADJ && SEL) v |= dbits(fabs(x)) > dbits(thr);
+            else v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
         }
         live = __any_sync(0xffffffffu, v);
     }

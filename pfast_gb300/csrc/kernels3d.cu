@@ -829,10 +829,14 @@ __global__ void tile_orders_kernel(const Sweep3Args A) {
 // the same value, so such a tile is a fixed point until a neighbour's change marks it.  That
 // holds bit for bit for the reference's updates too: every forward candidate from unreached
 // neighbours is at least INF, which the reference's MIN does not take over INF, and the
-// adjoint's POS/NEG terms of zero lambdas are +0 or -0, whose difference is +0.  One warp per
-// tile, lane = column of the box rows.
-template <typename Real, bool ADJ>
+// adjoint's POS/NEG terms of zero lambdas are +0 or -0, whose difference is +0.  FLOORED (the
+// adjoint polish): live only where some |lambda| exceeds a quarter of the polish floor -- an
+// update is a weighted sum of its upwind neighbours with weights summing to about 1, so in a
+// box of smaller values every correction stays within the floor and is dropped anyway.  One
+// warp per tile, lane = column of the box rows.
+template <typename Real, bool ADJ, bool FLOORED>
 __global__ void seed_tiles_kernel(const Sweep3Args A) {
+    const double thr = 0.25 * (double)A.polish_floor;   // FLOORED (adjoint polish): |lambda| above it
     const int tid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (tid >= A.ntiles) return;   // whole warps
     const int inst = A.act[blockIdx.y];
@@ -852,7 +856,8 @@ __global__ void seed_tiles_kernel(const Sweep3Args A) {
         for (int j = j0 - 1 + lane; j < j0 + TJ + 1; j += 32) {
             if ((unsigned)j >= (unsigned)nc) continue;
             const Real x = __ldg(row + j);
-            v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
+            if constexpr (FLOORED) v |= dbits(fabs(x)) > dbits(thr);
+            else v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
         }
         live = __any_sync(0xffffffffu, v);
     }
@@ -1039,11 +1044,11 @@ pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStr
     if (nact <= 0) return PFAST_OK;
     dim3 grid((unsigned)((a.ntiles + 7) / 8), nact);
     switch (kind) {
-        case kFwdPlain64: seed_tiles_kernel<double, false><<<grid, 256, 0, st>>>(a); break;
-        case kAdjPlain64: seed_tiles_kernel<double, true><<<grid, 256, 0, st>>>(a); break;
-        case kFwdFast32: seed_tiles_kernel<float, false><<<grid, 256, 0, st>>>(a); break;
-        case kAdjFast32: seed_tiles_kernel<float, true><<<grid, 256, 0, st>>>(a); break;
-        case kAdjPolish64: seed_tiles_kernel<double, true><<<grid, 256, 0, st>>>(a); break;
+        case kFwdPlain64: seed_tiles_kernel<double, false, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjPlain64: seed_tiles_kernel<double, true, false><<<grid, 256, 0, st>>>(a); break;
+        case kFwdFast32: seed_tiles_kernel<float, false, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjFast32: seed_tiles_kernel<float, true, false><<<grid, 256, 0, st>>>(a); break;
+        case kAdjPolish64: seed_tiles_kernel<double, true, true><<<grid, 256, 0, st>>>(a); break;
         default: return PFAST_OK;
     }
     cudaError_t e = cudaGetLastError();
