@@ -251,25 +251,27 @@ class Survey2D:
                                           self.nrec, ptr(rec), ptr(nx), ptr(tt), numofr, ptr(tr), ptr(Zc),
                                           C.byref(self._h)), "survey2d_create")
 
-    def forward(self, vp, precision=PFAST_PLAIN_FP64, maxswp=500, max_batch=0):
-        """Picks Tr [nrec, numofr+1] (transmission, then each reflector).  Returns (Tr, stats)."""
+    def forward(self, vp, precision=PFAST_PLAIN_FP64, maxswp=500, max_batch=0, near_source_radius=0):
+        """Picks Tr [nrec, numofr+1] (transmission, then each reflector).  Returns (Tr, stats).
+        near_source_radius > 0: opt-in straight-ray start of the nodes within that many nodes of
+        each source (not in the reference)."""
         import torch
         n = self.shape[0] * self.shape[1]
         Tr = torch.zeros((max(self.nrec, 1), self.numofr + 1), dtype=torch.float64, device=vp.device)
         st = _capi.Stats()
-        o = _opts(precision, maxswp, max_batch)
+        o = _opts(precision, maxswp, max_batch, near_source_radius=near_source_radius)
         check(lib().pfast_survey2d_forward(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
                                            Tr.data_ptr(), C.byref(st)), "survey2d_forward")
         return Tr[:self.nrec], st.as_dict()
 
-    def eval(self, vp, WR, precision=PFAST_PLAIN_FP64, maxswp=500, max_batch=0):
+    def eval(self, vp, WR, precision=PFAST_PLAIN_FP64, maxswp=500, max_batch=0, near_source_radius=0):
         """Joint gradient.  Returns dict(gT, gR, gRT, Et, Er, stats)."""
         import torch
         n = self.shape[0] * self.shape[1]
         gT, gR, gRT = (torch.empty(self.shape, dtype=torch.float64, device=vp.device) for _ in range(3))
         Et, Er = C.c_double(0), C.c_double(0)
         st = _capi.Stats()
-        o = _opts(precision, maxswp, max_batch)
+        o = _opts(precision, maxswp, max_batch, near_source_radius=near_source_radius)
         check(lib().pfast_survey2d_eval(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n),
                                         _dev_ptr(WR, "WR", numel=n), C.byref(o), gT.data_ptr(), gR.data_ptr(),
                                         gRT.data_ptr(), C.addressof(Et), C.addressof(Er), C.byref(st)),

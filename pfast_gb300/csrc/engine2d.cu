@@ -279,6 +279,14 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
     a.inst_lim = d.lim;
     a.inst_src = d.src;
     a.rowlim = sv->d_k2vec;
+    a.src_r2 = ctx->near_radius * ctx->near_radius;
+    // opt-in near-source start of the point-source instances (FP32 or FP64 fields)
+    auto near = [&](void* base, int is_fp32, const long long* off) -> pfast_status {
+        if (!init || ctx->near_radius <= 0) return PFAST_OK;
+        PFAST_LAUNCH(ctx, launch_near_source2(base, is_fp32, off, d.src, d.lim, sv->d_k2vec, s64, sv->nr, sv->nc,
+                                              sv->dx, sv->dz, ctx->near_radius, ninst, s));
+        return PFAST_OK;
+    };
     std::vector<int> active(ninst), iters(ninst, 0), caps(ninst, maxswp);
     for (int q = 0; q < ninst; ++q) active[q] = q;
     int dummy = 0;
@@ -286,6 +294,7 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
     long long* nu = st ? &st->fwd_node_updates : nullptr;
     if (precision == PFAST_PLAIN_FP64) {
         if (init) PFAST_LAUNCH(ctx, launch_init2(fields, 0, d.off, d.srcnode, N, ninst, s));
+        PFAST_TRY2(near(fields, 0, d.off));
         a.field = fields;
         a.inst_off = d.off;
         a.aux = s64;
@@ -303,6 +312,7 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
         float* snap32 = f32 + N * ninst;
         if (init) PFAST_LAUNCH(ctx, launch_init2(f32, 1, d.off32, d.srcnode, N, ninst, s));
         else PFAST_LAUNCH(ctx, launch_narrow_inst(fields, f32, d.off, d.off32, N, ninst, s));
+        PFAST_TRY2(near(f32, 1, d.off32));
         a.field = f32;
         a.inst_off = d.off32;
         a.aux = s32;
@@ -312,6 +322,7 @@ pfast_status fwd_phase2(pfast_ctx* ctx, pfast_survey2d* sv, double* fields, cons
                                st ? &st->ms_fwd32 : nullptr));
         if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
         PFAST_LAUNCH(ctx, launch_widen_inst(f32, fields, d.off32, d.off, N, ninst, s));
+        PFAST_TRY2(near(fields, 0, d.off));   // the fixed region keeps its FP64 values in the polish
         active.resize(ninst);
         for (int q = 0; q < ninst; ++q) { active[q] = q; iters[q] = 0; }
         a.field = fields;
@@ -609,6 +620,11 @@ pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp
     o.schedule = PFAST_SCHEDULE_AUTO;
     o.near_source_radius = 0;
     if (opt) o = *opt;
+    if (o.near_source_radius < 0 || o.near_source_radius > 64) {
+        set_last_error("near_source_radius must be in [0, 64]");
+        return PFAST_ERR_INVALID;
+    }
+    ctx->near_radius = o.near_source_radius;
     if (st) std::memset(st, 0, sizeof(*st));
     if (sv->geom_status) {
         set_last_error(sv->geom_status == PFAST_ERR_INVALID ? "survey has no reflector geometry"
@@ -667,6 +683,11 @@ pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, c
     o.schedule = PFAST_SCHEDULE_AUTO;
     o.near_source_radius = 0;
     if (opt) o = *opt;
+    if (o.near_source_radius < 0 || o.near_source_radius > 64) {
+        set_last_error("near_source_radius must be in [0, 64]");
+        return PFAST_ERR_INVALID;
+    }
+    ctx->near_radius = o.near_source_radius;
     if (st) std::memset(st, 0, sizeof(*st));
     if (!sv->has_picks) { set_last_error("survey has no picks: gradient unavailable"); return PFAST_ERR_INVALID; }
     if (sv->geom_status) { set_last_error("no node above a reflector (reflector geometry)"); return sv->geom_status; }

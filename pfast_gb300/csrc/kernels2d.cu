@@ -396,7 +396,9 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
             const int c = cb + lj;
             const int gj = j0 + lj;
             if constexpr (!ADJ) {
-                const bool upd = (rl == nullptr || gi <= __ldg(rl + gj)) && !(gi == si && gj == sj);
+                // the source node (and the opt-in fixed region around it) keeps its value
+                const bool upd = (rl == nullptr || gi <= __ldg(rl + gj)) &&
+                                 (si < 0 || (gi - si) * (gi - si) + (gj - sj) * (gj - sj) > A.src_r2);
                 if (upd) {
                     const Real old = box[c];
                     Real nv = old;
@@ -770,6 +772,45 @@ void free_diag_table2(DiagTable2& t) {
     if (t.d_tiles) cudaFree(t.d_tiles);
     t.d_off = nullptr;
     t.d_tiles = nullptr;
+}
+
+template <typename Real>
+__global__ void near_source2_kernel(Real* __restrict__ base, const long long* __restrict__ off,
+                                    const int* __restrict__ inst_src, const int* __restrict__ inst_lim,
+                                    const int* __restrict__ rowlim, const double* __restrict__ s64, int nr, int nc,
+                                    double dx, double dz, int r) {
+    const int q = blockIdx.y;
+    if (inst_src[q] < 0) return;
+    const int si = inst_src[q] >> 16, sj = inst_src[q] & 0xffff;
+    const int* rl = inst_lim[q] >= 0 ? rowlim + (long long)inst_lim[q] * nc : nullptr;
+    const double ss = s64[(long long)si * nc + sj];
+    const int w = 2 * r + 1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w * w; t += gridDim.x * blockDim.x) {
+        const int qi = t / w - r, qj = t % w - r;
+        const int i = si + qi, j = sj + qj;
+        if (i < 0 || i >= nr || j < 0 || j >= nc || qi * qi + qj * qj > r * r) continue;
+        if (rl != nullptr && i > rl[j]) continue;   // below the reflector: not part of this solve
+        const long long node = (long long)i * nc + j;
+        const double ez = qi * dz, ex = qj * dx;
+        base[off[q] + node] = Real(0.5 * (ss + s64[node]) * sqrt(ez * ez + ex * ex));
+    }
+}
+
+pfast_status launch_near_source2(void* base, int is_fp32, const long long* off, const int* inst_src,
+                                 const int* inst_lim, const int* rowlim, const double* s64, int nr, int nc, double dx,
+                                 double dz, int radius, int ninst, cudaStream_t st) {
+    if (radius <= 0 || ninst <= 0) return PFAST_OK;
+    const int w = 2 * radius + 1;
+    dim3 grid((unsigned)std::max(1, (w * w + 255) / 256), ninst);
+    if (is_fp32)
+        near_source2_kernel<float><<<grid, 256, 0, st>>>((float*)base, off, inst_src, inst_lim, rowlim, s64, nr, nc, dx,
+                                                         dz, radius);
+    else
+        near_source2_kernel<double><<<grid, 256, 0, st>>>((double*)base, off, inst_src, inst_lim, rowlim, s64, nr, nc,
+                                                          dx, dz, radius);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "near_source2 launch", __FILE__, __LINE__);
+    return PFAST_OK;
 }
 
 pfast_status launch_seed_tiles2(int kind, const Sweep2Args& a, int nact, cudaStream_t st) {

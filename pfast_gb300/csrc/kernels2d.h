@@ -34,6 +34,8 @@ struct Sweep2Args {
     float dxf, dzf;              // FP32 copies of dx, dz (no FP64 instruction in the FP32 sweeps)
     float wxf, wzf, rsumf;       // FP32 inv2x, inv2z, 1/(inv2x + inv2z)
     float polish_floor;          // polish corrections at or below this are dropped
+    int src_r2;                  // forward: nodes within squared node distance src_r2 of the source
+                                 // are fixed (0: the source node alone, the reference's point source)
     int dir;                     // 0..3: bit1 = s1>0 (rows), bit0 = s2>0 (cols); reference order
     int iter;                    // outer iteration (snapshot stamps)
     int ntiles;                  // tiles per instance (nbi * nbj)
@@ -56,6 +58,13 @@ struct DiagTable2 {
 pfast_status build_diag_table2(int nr, int nc, DiagTable2& t);
 void free_diag_table2(DiagTable2& t);
 pfast_status launch_sweep2(int kind, const Sweep2Args& a, int d, int tiles, int nact, cudaStream_t st);
+// Opt-in near-source start (not in the reference): in each instance q with a point source
+// (inst_src[q] >= 0), the nodes within `radius` nodes (Euclidean) get the straight-ray time
+// 0.5 (s_src + s_node) * distance; a down-going instance (inst_lim[q] >= 0) only above its
+// reflector row limit.  Fields (FP32 if is_fp32) at base + off[q].
+pfast_status launch_near_source2(void* base, int is_fp32, const long long* off, const int* inst_src,
+                                 const int* inst_lim, const int* rowlim, const double* s64, int nr, int nc, double dx,
+                                 double dz, int radius, int ninst, cudaStream_t st);
 // Initial lock words from the starting field (active instances a.act[0..nact)): due where the
 // tile's halo box holds a reached traveltime / nonzero lambda.  The forward polish: no-op.
 pfast_status launch_seed_tiles2(int kind, const Sweep2Args& a, int nact, cudaStream_t st);
