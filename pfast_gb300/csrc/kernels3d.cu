@@ -113,6 +113,33 @@ __device__ __forceinline__ float eik3_fast(float a, float b, float c, float s, c
     return (D3 >= 0.f) ? c + (fmaf(wa, A, wbB) + sqrtf(D3)) * K.rWf : (float)kInf;
 }
 
+// Square root by the hardware approximation (PTX sqrt.approx.f32, a few ulps): the FP32 bulk
+// result is only the starting point of the FP64 polish.
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The same solution on an isotropic grid (one spacing h): unit weights, sh = s h, the three
+// neighbour minima sorted by min/max (values >= 0 or +inf: no NaN arises), so
+//   2 terms: x = (B + sqrt(2 sh^2 - B^2)) / 2
+//   3 terms: x = (A + B + sqrt(3 sh^2 - (A-B)^2 - A^2 - B^2)) / 3.
+__device__ __forceinline__ float eik3_fast_iso(float a, float b, float c, float sh) {
+    const float lo = fminf(a, b), hi = fmaxf(a, b);
+    const float c0 = fminf(lo, c), mid = fmaxf(lo, c);
+    const float b0 = fminf(hi, mid), a0 = fmaxf(hi, mid);
+    float q = c0 + sh;
+    if (q <= b0) return q;
+    const float B = b0 - c0;
+    const float D = fmaf(2.0f * sh, sh, -B * B);
+    q = (D >= 0.f) ? fmaf(0.5f, B + sqrt_approx(D), c0) : (float)kInf;
+    if (q <= a0) return q;
+    const float A = a0 - c0, AB = A - B;
+    const float D3 = fmaf(3.0f * sh, sh, -fmaf(AB, AB, fmaf(A, A, B * B)));
+    return (D3 >= 0.f) ? fmaf(1.0f / 3.0f, (A + B) + sqrt_approx(D3), c0) : (float)kInf;
+}
+
 // FP64 polish Godunov update: one Newton step from the current value U0 on
 //   f(q) = sum_m w_m max(q - a_m, 0)^2 - s^2,
 // whose root is the Godunov value (the 1-, 2- and 3-term cases of
@@ -194,8 +221,18 @@ __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float
                                            const Spacing3& sp) {
     const float ti = (float)kInf;
     if (T0 >= ti || Txp >= ti || Txm >= ti || Typ >= ti || Tym >= ti || Tzp >= ti || Tzm >= ti) return 0.f;
-    const float wx = sp.wf[0], wy = sp.wf[1], wz = sp.wf[2];
     float e, den, num;
+    if (sp.iso) {   // one weight: it cancels in num / den
+        e = Txp - T0; den = fmaxf(-e, 0.f); num = fmaxf(e, 0.f) * Lxp;
+        e = Txm - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lxm, num);
+        e = Typ - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lyp, num);
+        e = Tym - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lym, num);
+        e = Tzp - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lzp, num);
+        e = Tzm - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lzm, num);
+        const float r = (den * sp.wf[0] > 1e-9f) ? __fdividef(num, den) : 0.f;
+        return fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r;
+    }
+    const float wx = sp.wf[0], wy = sp.wf[1], wz = sp.wf[2];
     e = Txp - T0; den = wx * fmaxf(-e, 0.f); num = wx * fmaxf(e, 0.f) * Lxp;
     e = Txm - T0; den = fmaf(wx, fmaxf(-e, 0.f), den); num = fmaf(wx * fmaxf(e, 0.f), Lxm, num);
     e = Typ - T0; den = fmaf(wy, fmaxf(-e, 0.f), den); num = fmaf(wy * fmaxf(e, 0.f), Lyp, num);
@@ -528,10 +565,11 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                         const double zc = min_nonneg(box[c - PS], box[c + PS]);
                         nv = min_nonneg(old, eik3_plain(xa, yb, zc, s, A.sp));
                     } else if constexpr (KIND == kFwdFast32) {
-                        const float xa = ref_min(box[c + 1], box[c - 1]);
-                        const float yb = ref_min(box[c - HJ], box[c + HJ]);
-                        const float zc = ref_min(box[c - PS], box[c + PS]);
-                        nv = ref_min(old, eik3_fast(xa, yb, zc, s, A.sp));
+                        // field values are >= +0 or +inf: fminf is the reference's MIN here
+                        const float xa = fminf(box[c + 1], box[c - 1]);
+                        const float yb = fminf(box[c - HJ], box[c + HJ]);
+                        const float zc = fminf(box[c - PS], box[c + PS]);
+                        nv = fminf(old, A.sp.iso ? eik3_fast_iso(xa, yb, zc, s * A.sp.df[0]) : eik3_fast(xa, yb, zc, s, A.sp));
                     } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2, (s h)^2 when isotropic)
                         // Octant selection: if an axis is active (U0 above its smaller neighbour) and
                         // that neighbour is the one this sweep visits after the node, the update would
