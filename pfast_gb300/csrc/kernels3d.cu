@@ -54,7 +54,6 @@ __host__ __device__ constexpr int warp_smem_bytes() {
                (T::adj && !t_windows<KIND>() ? HK * PS * sizeof(typename T::Aux) : 0));
 }
 
-__device__ __forceinline__ float ref_min(float x, float y) { return (x < y) ? x : y; }
 
 
 // ----------------------------------------------------------- node updates
