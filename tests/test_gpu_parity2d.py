@@ -216,3 +216,31 @@ def test_near_source_initialisation_2d(ctx):
     with pytest.raises(pg.PfastError):
         sv.forward(d, precision=pg.PFAST_PLAIN_FP64, near_source_radius=65)
     sv.close()
+
+
+def test_joint_gradient_full_size(ctx):
+    """The 2D joint inversion workload at full size (601 x 201 grid, h = 5 m, 40 sources, 400
+    receivers, one reflector): the plain joint gradient equals the oracle bit for bit; the mixed
+    one stays within 1e-4 relative L2 of it, with the misfits within 1e-6."""
+    from oracle import port
+    from pfast_gb300 import inv_bench
+    pg, torch = _pg(), _torch()
+    vt, v0, Z, src, srnum, rec, nxy = inv_bench.workload()
+    nr, nc = vt.shape
+    assert (nr, nc) == (201, 601) and len(srnum) == 40 and int(srnum[0]) == 400
+    tt, tr = inv_bench.picks(ctx, vt, Z, src, srnum, rec)
+    WR = np.full((nr, nc), 0.5)
+    r0 = port.eval2d(v0, WR, Z, src, srnum, rec, nxy, tt, tr, 1, 500, inv_bench.H, inv_bench.H, nthreads=4)
+    sv = pg.Survey2D(ctx, nr, nc, inv_bench.H, inv_bench.H, src, srnum, rec, numofr=1, Z=Z, nxy=nxy,
+                     tt_obs=tt, tr_obs=tr)
+    d, w = torch.from_numpy(v0).cuda(), torch.from_numpy(WR).cuda()
+    rp = sv.eval(d, w, precision=pg.PFAST_PLAIN_FP64)
+    for k in ("gT", "gR", "gRT"):
+        assert bits_equal(rp[k].cpu().numpy(), r0[k]), k
+    assert rp["Et"] == r0["Et"] and rp["Er"] == r0["Er"]
+    rm = sv.eval(d, w, precision=pg.PFAST_MIXED)
+    sv.close()
+    for k in ("gT", "gR", "gRT"):
+        g, g0 = rm[k].cpu().numpy(), r0[k]
+        assert np.linalg.norm(g - g0) <= 1e-4 * np.linalg.norm(g0), k
+    assert abs(rm["Et"] - r0["Et"]) <= 1e-6 * abs(r0["Et"]) and abs(rm["Er"] - r0["Er"]) <= 1e-6 * abs(r0["Er"])

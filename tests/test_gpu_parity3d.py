@@ -324,3 +324,46 @@ def test_graph_replay_matches_launches(ctx, precision):
     assert bits_equal(g0.cpu().numpy(), g2.cpu().numpy()) and e0 == e2
     for k in ("fwd_iters_max", "adj_iters_max", "fwd32_iters_max", "adj32_iters_max", "launches"):
         assert s0[k] == s1[k] == s2[k], k
+
+
+def test_full_size_grid(ctx):
+    """The grid of the 3D gradient workload at full size (256 x 256 x 128 nodes, h = 20 m, 4096
+    receivers per source), with 4 sources: plain FP64 equals the oracle on one source (gradient,
+    misfit and picks bit for bit); mixed stays within the tolerances of plain on all four; the
+    mixed bits do not depend on the batch split."""
+    from oracle import port
+    from pfast_gb300 import workloads
+    pg, torch = _pg(), _torch()
+    vt, v0, src, srnum, rec, nxyz = workloads.c3_inputs(n_src_side=2, n_rec_side=64)
+    nz, nr, nc = v0.shape
+    h = workloads.H
+    assert (nz, nr, nc) == (128, 256, 256) and len(srnum) == 4 and srnum[0] == 4096
+    tobs = workloads.observed_picks(ctx, vt, src, srnum, rec, pg.PFAST_PLAIN_FP64)
+    d = torch.from_numpy(v0).cuda()
+
+    # one source, plain, against the oracle
+    n0 = int(srnum[0])
+    sv1 = pg.Survey3D(ctx, nr, nc, nz, h, h, h, src[:1], srnum[:1], rec[:n0], nxyz[:n0], tobs[:n0])
+    g1, e1, _ = sv1.eval(d, precision=pg.PFAST_PLAIN_FP64)
+    p1, _ = sv1.forward(d, precision=pg.PFAST_PLAIN_FP64)
+    sv1.close()
+    g_ref, e_ref, _, _ = port.eval3d(v0, src[:1], srnum[:1], rec[:n0], nxyz[:n0], tobs[:n0], 100, h, h, h)
+    p_ref = port.forward3d(v0, src[:1], srnum[:1], rec[:n0], 100, h, h, h)
+    assert bits_equal(g1.cpu().numpy(), g_ref) and e1 == e_ref
+    assert bits_equal(p1.cpu().numpy(), p_ref)
+
+    # four sources: mixed against plain, and the batch split
+    sv = pg.Survey3D(ctx, nr, nc, nz, h, h, h, src, srnum, rec, nxyz, tobs)
+    gp, ep, _ = sv.eval(d, precision=pg.PFAST_PLAIN_FP64)
+    pp, _ = sv.forward(d, precision=pg.PFAST_PLAIN_FP64)
+    gm, em, _ = sv.eval(d, precision=pg.PFAST_MIXED)
+    gm1, em1, st1 = sv.eval(d, precision=pg.PFAST_MIXED, max_batch=1)
+    pm, _ = sv.forward(d, precision=pg.PFAST_MIXED)
+    sv.close()
+    gp, gm, pp, pm = gp.cpu().numpy(), gm.cpu().numpy(), pp.cpu().numpy(), pm.cpu().numpy()
+    assert np.all(np.isfinite(pm)) and np.all(pm > 0)
+    assert np.max(np.abs(pm - pp) / pp) <= TT_REL_TOL
+    assert np.linalg.norm(gm - gp) / np.linalg.norm(gp) <= GRAD_REL_L2_TOL
+    assert abs(em - ep) <= 1e-6 * abs(ep)
+    assert st1["batches"] == 4
+    assert bits_equal(gm, gm1.cpu().numpy()) and em == em1
