@@ -453,14 +453,13 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         }
     } else {
         float* T32 = ctx->scratch.as<float>();
-        float* snap32 = T32 + N * nb;
         PFAST_LAUNCH(ctx, launch_init_fwd3(T32, 1, N, N, src_lin, nb, s));
         if (ctx->near_radius > 0)
             PFAST_LAUNCH(ctx, launch_near_source3(T32, 1, N, a.src_kij, ctx->s64.as<double>(), sv->nz, sv->nr, sv->nc,
                                                   a.sp, ctx->near_radius, nb, s));
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = T32;
-        a.snap = snap32;
+        a.snap = nullptr;   // the FP32 bulk kinds keep no snapshot
         a.aux = ctx->s32.p;
         a.tol_abs_f = 0.0f;
         a.tol_rel_f = (float)kTol32Rel;
@@ -567,12 +566,11 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     } else {
         std::vector<int> active64 = active;
         float* L32 = ctx->scratch.as<float>();
-        float* snap32 = L32 + N * nb;
         PFAST_TRY(ctx->T32.ensure(sizeof(float) * N * nb));
         PFAST_LAUNCH(ctx, launch_narrow(ctx->L64.as<double>(), L32, N, N, N, nb, s));
         PFAST_LAUNCH(ctx, launch_narrow(ctx->T64.as<double>(), ctx->T32.as<float>(), N, N, N, nb, s));
         a.field = L32;
-        a.snap = snap32;
+        a.snap = nullptr;   // the FP32 bulk kinds keep no snapshot
         a.aux = ctx->T32.p;
         a.tol_abs_f = (float)kTol32AbsAdj;
         a.tol_rel_f = (float)kTol32Rel;

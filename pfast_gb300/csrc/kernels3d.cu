@@ -408,9 +408,16 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     int* dirty = A.dirty + (long long)inst * A.ntiles;
     const int obit = 1 << dir;
     constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
+    // Convergence test of the FP32 bulk kinds: a node that moved by more than the FP32
+    // tolerance in some processing of this outer iteration (the flag is ORed over the
+    // iteration's processings).  The other kinds compare with a snapshot taken at the tile's
+    // first processing in the iteration, as the reference's isconv does.
+    constexpr bool kSnap = !(KIND == kFwdFast32 || KIND == kAdjFast32);
+    // The tile's lock word as lane 0 last wrote it.  Face neighbours run in other launches and
+    // no other tile of this launch writes it, so it is composed here without reading it back.
+    int dword = kSelective ? (dmask & ~obit) : 0;
     if (lane == 0) {
-
-        dirty[tid] = kSelective ? (dmask & ~obit) : 0;   // face neighbours run in other launches: no race
+        dirty[tid] = dword;
         if (A.work) atomicAdd(A.work + inst, (unsigned long long)(min(TK, A.nz - tk * TK) * min(TI, A.nr - ti * TI) *
                                                                   min(TJ, A.nc - tj * TJ)));
     }
@@ -424,7 +431,6 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     Aux* aux = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
     constexpr bool TWIN = t_windows<KIND>();
     Real* fld = reinterpret_cast<Real*>(A.field) + inst * A.fstride;
-    Real* snp = reinterpret_cast<Real*>(A.snap) + inst * A.fstride;
 
     // ---- stage the field halo box (out-of-grid: +inf for the forward so that the
     // neighbour minimum reduces to the one-sided rule at faces; never read by the adjoint)
@@ -447,16 +453,19 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
     // ---- snapshot at the tile's first processing in this outer iteration (its values are
     // still the iteration-start values then: only the tile itself writes them)
-    int* stamp = A.stamp + (long long)inst * A.ntiles;
-    if (__ldcg(stamp + tid) != iter) {
+    Real* snp = kSnap ? reinterpret_cast<Real*>(A.snap) + inst * A.fstride : nullptr;
+    if constexpr (kSnap) {
+        int* stamp = A.stamp + (long long)inst * A.ntiles;
+        if (__ldcg(stamp + tid) != iter) {
 #pragma unroll 4
-        for (int m = 0; m < 32; ++m) {
-            const int rk = m / TI, ri = m % TI;
-            if (rk < ek && ri < ei && lane < ej)
-                snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
-                    box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+            for (int m = 0; m < 32; ++m) {
+                const int rk = m / TI, ri = m % TI;
+                if (rk < ek && ri < ei && lane < ej)
+                    snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
+                        box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+            }
+            if (lane == 0) stamp[tid] = iter;
         }
-        if (lane == 0) stamp[tid] = iter;
     }
     __syncwarp();
 
@@ -481,6 +490,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     // FP32 bulk: some changed node feeds an in-tile node that this pass visited before it
     // (so the tile is not yet a fixed point of the update)
     bool stale = false;
+    bool moved = false;   // FP32 bulk: some node of this lane moved by more than the tolerance
 
     // ---- adjoint traveltime windows (FP64 kinds).  Lane (kf, if) (flipped coordinates) is at flipped
     // position jf = t - kf - if in step t and keeps its pencil's traveltimes at jf-1, jf, jf+1
@@ -621,6 +631,8 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             if (bo != bn) {
                 box[c] = nv;
                 chg = true;
+                if constexpr (!kSnap)
+                    if (fabsf(old - nv) > A.tol_abs_f + A.tol_rel_f * fabsf(nv)) moved = true;
                 if constexpr (kPrune) {
                     // the neighbour node across a face (box index n, traveltime tn): does it
                     // depend on this node?
@@ -656,7 +668,8 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
     if constexpr (kSelective) {
         const unsigned tsel = __reduce_or_sync(0xffffffffu, sel);
-        if (lane == 0) dirty[tid] = (dirty[tid] & 0xff) | (int)(tsel << 8);
+        dword = (dword & 0xff) | (int)(tsel << 8);
+        if (lane == 0) dirty[tid] = dword;
     }
 
     // ---- nothing changed: the field and its snapshot comparison stand as they are
@@ -682,7 +695,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
         // neighbours keep their selection bits: OR in the eight order bits (two tiles of one
         // launch can share a face neighbour, hence atomic)
         const int sk_ = A.nbi * A.nbj;
-        dirty[tid] |= again ? 0xff : (kSelective ? (0xff & ~obit) : 0);
+        dirty[tid] = dword | (again ? 0xff : (kSelective ? (0xff & ~obit) : 0));
         if (f_klo && tk > 0) atomicOr(dirty + tid - sk_, 0xff);
         if (f_khi && tk < A.nbk - 1) atomicOr(dirty + tid + sk_, 0xff);
         if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xff);
@@ -691,33 +704,38 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
         if (f_jhi && tj < A.nbj - 1) atomicOr(dirty + tid + 1, 0xff);
     }
 
-    // ---- write back and compare with the iteration-start snapshot
-    bool moved = false;
-#pragma unroll 1
-    for (int m0 = 0; m0 < 32; m0 += 8) {
-        Real p[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int m = m0 + u, rk = m / TI, ri = m % TI;
-            p[u] = Real(0);
-            if (rk < ek && ri < ei && lane < ej) p[u] = __ldcg(snp + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane);
+    // ---- write back; the FP64 kinds compare with the iteration-start snapshot
+    if constexpr (!kSnap) {
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
+            const int rk = m / TI, ri = m % TI;
+            if (rk < ek && ri < ei && lane < ej)
+                fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
         }
+        if (__any_sync(0xffffffffu, moved) && lane == 0) A.diff[(long long)inst * A.ntiles + tid] = 1;
+    } else {
+#pragma unroll 1
+        for (int m0 = 0; m0 < 32; m0 += 8) {
+            Real p[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int m = m0 + u, rk = m / TI, ri = m % TI;
-            if (rk < ek && ri < ei && lane < ej) {
-                const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
-                fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = v;
-                if constexpr (sizeof(Real) == 8) {
+            for (int u = 0; u < 8; ++u) {
+                const int m = m0 + u, rk = m / TI, ri = m % TI;
+                p[u] = Real(0);
+                if (rk < ek && ri < ei && lane < ej) p[u] = __ldcg(snp + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int m = m0 + u, rk = m / TI, ri = m % TI;
+                if (rk < ek && ri < ei && lane < ej) {
+                    const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+                    fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = v;
                     if (fabs(p[u] - v) > A.tol_abs) moved = true;   // isconv, src/T_pfsm3d.h:126
-                } else {
-                    if (fabsf(p[u] - v) > A.tol_abs_f + A.tol_rel_f * fabsf(v)) moved = true;
                 }
             }
         }
+        const bool any_moved = __any_sync(0xffffffffu, moved);
+        if (lane == 0) A.diff[(long long)inst * A.ntiles + tid] = any_moved ? 1 : 0;
     }
-    const bool any_moved = __any_sync(0xffffffffu, moved);
-    if (lane == 0) A.diff[(long long)inst * A.ntiles + tid] = any_moved ? 1 : 0;
 }
 
 // One launch per tile diagonal: block (x, y) = (tile of the diagonal, active instance).

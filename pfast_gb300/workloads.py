@@ -42,13 +42,19 @@ def main():
     p.add_argument("--sources", type=int, default=16, help="number of sources (a square number)")
     p.add_argument("--precision", choices=["plain", "mixed"], default="mixed")
     p.add_argument("--evals", type=int, default=1)
+    p.add_argument("--picks-precision", choices=["plain", "mixed"], default="mixed",
+                   help="solver of the observed picks (plain: the evaluation is the only user of the mixed kernels)")
+    p.add_argument("--no-graphs", action="store_true", help="launch the sweeps one by one (kernel indices for ncu -s)")
     a = p.parse_args()
     side = int(round(np.sqrt(a.sources)))
     nz, nr, nc = a.grid
     vt, v0, src, srnum, rec, nxyz = c3_inputs(nz, nr, nc, side, max(1, nr // 4))
     ctx = api.Context(0)
+    if a.no_graphs:
+        ctx.set_graphs(False)
     prec = api.PFAST_MIXED if a.precision == "mixed" else api.PFAST_PLAIN_FP64
-    tobs = observed_picks(ctx, vt, src, srnum, rec, api.PFAST_MIXED)
+    pprec = api.PFAST_MIXED if a.picks_precision == "mixed" else api.PFAST_PLAIN_FP64
+    tobs = observed_picks(ctx, vt, src, srnum, rec, pprec)
     sv = api.Survey3D(ctx, nr, nc, nz, H, H, H, src, srnum, rec, nxyz, tobs)
     d = torch.from_numpy(v0).cuda()
     for _ in range(a.evals):
