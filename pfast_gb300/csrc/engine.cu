@@ -474,7 +474,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         active.resize(nb);
         for (int b = 0; b < nb; ++b) active[b] = b;
         a.field = ctx->T64.p;
-        a.snap = ctx->scratch.p;
+        a.snap = nullptr;   // the polish kinds keep no snapshot
         a.aux = ctx->sq64.p;
         a.slow64 = ctx->s64.as<double>();
         a.polish_floor = ctx->polish_floor;
@@ -581,7 +581,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
                                       sv->nr, sv->nc, wpr, nb, s));
         std::fill(iters.begin(), iters.end(), 0);
         a.field = ctx->L64.p;
-        a.snap = ctx->scratch.p;
+        a.snap = nullptr;   // the polish kinds keep no snapshot
         a.aux = ctx->T64.p;
         a.polish_floor = ctx->polish_floor;
         a.tol_abs = kConvTol;

@@ -148,7 +148,8 @@ __device__ __forceinline__ float eik3_fast_iso(float a, float b, float c, float 
 // big: the step leaves a second-order remainder (about sum_active(w) step^2 / f') above the
 // floor, so the node wants another Newton step in the same order.
 __device__ __forceinline__ double eik3_newton(double U0, double a, double b, double c, double s2, const double* slow,
-                                              long long node, const Spacing3& sp, float floor, bool& big) {
+                                              long long node, const Spacing3& sp, float floor, bool& big,
+                                              float& dstep) {
     // FP64 for what fixes the root (the differences and the residual f, 7 FP64 instructions
     // in the isotropic case); the derivative f' and the step in FP32.  Isotropic grids: s2 holds
     // (s h)^2 and f is the residual divided by 1/h^2 (same root, unit weights).
@@ -166,6 +167,7 @@ __device__ __forceinline__ double eik3_newton(double U0, double a, double b, dou
     const float fp = 2.0f * (wx * fx + wy * fy + wz * fz);
     if (!(fp > 0.0f)) {
         big = true;
+        dstep = INFINITY;   // a restart: the change is not a Newton step
         const double s = __ldg(slow + node);
         return fmin(fma(sp.d[0], s, a), fmin(fma(sp.d[1], s, b), fma(sp.d[2], s, c)));
     }
@@ -173,6 +175,7 @@ __device__ __forceinline__ double eik3_newton(double U0, double a, double b, dou
     const float sw = (dbits(px) > 0 ? wx : 0.0f) + (dbits(py) > 0 ? wy : 0.0f) +
                      (dbits(pz) > 0 ? wz : 0.0f);   // p >= 0: integer tests keep the FP64 pipe free
     big = sw * step * step > floor * fp;
+    dstep = fabsf(step);   // the change of the node, to FP32 precision
     // corrections far below the 1e-9 convergence tolerance are dropped, so that a
     // converged region reaches a bitwise fixed point (and its tiles lock)
     return fabsf(step) <= floor ? U0 : U0 - widen_exact(step);
@@ -250,7 +253,9 @@ __device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float
 // r = 0 in FP64.  13 FP64 instructions in the isotropic case.
 __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm, double Typ, double Tym, double Tzp,
                                               double Tzm, double Lxp, double Lxm, double Lyp, double Lym, double Lzp,
-                                              double Lzm, double L0, const Spacing3& sp, float floor, bool& big) {
+                                              double Lzm, double L0, const Spacing3& sp, float floor, bool& big,
+                                              float& dstep) {
+    dstep = INFINITY;   // the branches that reset lambda to 0
     if (unreached64(T0, Txp, Txm, Typ, Tym, Tzp, Tzm)) return 0.0;
     const double exp_ = Txp - T0, exm = Txm - T0, eyp = Typ - T0, eym = Tym - T0, ezp = Tzp - T0, ezm = Tzm - T0;
     auto mu = [&](double e, double L) { return __double2hiint(e) < 0 ? L0 : L; };
@@ -273,6 +278,7 @@ __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm,
     const float step = __fdividef(narrow_trunc(r), den);
     const float tol = floor * (1.0f + fabsf(narrow_trunc(L0)));
     big = fabsf(step) * 1.2e-7f > tol;   // the local equation is linear: only the FP32 step's error remains
+    dstep = fabsf(step);
     return fabsf(step) <= tol ? L0 : L0 + widen_exact(step);
 }
 
@@ -408,11 +414,12 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     int* dirty = A.dirty + (long long)inst * A.ntiles;
     const int obit = 1 << dir;
     constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
-    // Convergence test of the FP32 bulk kinds: a node that moved by more than the FP32
+    // Convergence test of the FP32 bulk and polish kinds: a node that moved by more than the
     // tolerance in some processing of this outer iteration (the flag is ORed over the
-    // iteration's processings).  The other kinds compare with a snapshot taken at the tile's
-    // first processing in the iteration, as the reference's isconv does.
-    constexpr bool kSnap = !(KIND == kFwdFast32 || KIND == kAdjFast32);
+    // iteration's processings; a polish change is its FP32 step, so the test needs no FP64
+    // instruction).  The plain kinds compare with a snapshot taken at the tile's first
+    // processing in the iteration, as the reference's isconv does.
+    constexpr bool kSnap = KIND == kFwdPlain64 || KIND == kAdjPlain64;
     // The tile's lock word as lane 0 last wrote it.  Face neighbours run in other launches and
     // no other tile of this launch writes it, so it is composed here without reading it back.
     int dword = kSelective ? (dmask & ~obit) : 0;
@@ -490,7 +497,8 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     // FP32 bulk: some changed node feeds an in-tile node that this pass visited before it
     // (so the tile is not yet a fixed point of the update)
     bool stale = false;
-    bool moved = false;   // FP32 bulk: some node of this lane moved by more than the tolerance
+    bool moved = false;   // FP32 bulk, polish: some node of this lane moved by more than the tolerance
+    const float tol_step = (float)A.tol_abs;
 
     // ---- adjoint traveltime windows (FP64 kinds).  Lane (kf, if) (flipped coordinates) is at flipped
     // position jf = t - kf - if in step t and keeps its pencil's traveltimes at jf-1, jf, jf+1
@@ -560,6 +568,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             const int gj = j0 + lj;
             const Real old = box[c];
             Real nv = old;
+            float dstep = INFINITY;   // polish: the size of this node's change
             if constexpr (ADJ && !TWIN) {   // FP32 bulk: the traveltimes from the staged box
                 t0 = aux[c]; Txm = aux[c - 1]; Txp = aux[c + 1]; Tym = aux[c - HJ]; Typ = aux[c + HJ];
                 Tzm = aux[c - PS]; Tzp = aux[c + PS];
@@ -595,7 +604,8 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                             const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
                             const double zc = min_nonneg(box[c - PS], box[c + PS]);
                             bool big = false;
-                            nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp, A.polish_floor, big);
+                            nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp, A.polish_floor, big,
+                                             dstep);
                             restep |= big;
                         }
                     }
@@ -619,7 +629,8 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                         if (m & obit) {
                             bool big = false;
                             nv = adj3_polish(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
-                                             box[c - HJ], box[c + PS], box[c - PS], old, A.sp, A.polish_floor, big);
+                                             box[c - HJ], box[c + PS], box[c - PS], old, A.sp, A.polish_floor, big,
+                                             dstep);
                             restep |= big;
                         }
                     }
@@ -631,8 +642,11 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             if (bo != bn) {
                 box[c] = nv;
                 chg = true;
-                if constexpr (!kSnap)
+                if constexpr (kSelective) {
+                    if (dstep > tol_step) moved = true;
+                } else if constexpr (!kSnap) {
                     if (fabsf(old - nv) > A.tol_abs_f + A.tol_rel_f * fabsf(nv)) moved = true;
+                }
                 if constexpr (kPrune) {
                     // the neighbour node across a face (box index n, traveltime tn): does it
                     // depend on this node?
