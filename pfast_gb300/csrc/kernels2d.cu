@@ -116,7 +116,8 @@ __device__ __forceinline__ float adj2_bulk(float T0, float Txp, float Txm, float
 // leaves a remainder above the floor.
 __device__ __forceinline__ double adj2_polish(double T0, double Txp, double Txm, double Tzp, double Tzm, double Lxp,
                                               double Lxm, double Lzp, double Lzm, double L0, double wx, double wz,
-                                              float wxf, float wzf, float floor, bool& big) {
+                                              float wxf, float wzf, float floor, bool& big, float& dstep) {
+    dstep = INFINITY;   // the branches that reset lambda to 0
     const long long inf = dbits(kInf);   // T >= INF on the bit patterns (T >= 0)
     if (dbits(Txp) >= inf || dbits(T0) >= inf || dbits(Txm) >= inf || dbits(Tzp) >= inf || dbits(Tzm) >= inf)
         return 0.0;
@@ -130,6 +131,7 @@ __device__ __forceinline__ double adj2_polish(double T0, double Txp, double Txm,
     const float step = __fdividef(narrow_trunc(r), den);
     const float tol = floor * (1.0f + fabsf(narrow_trunc(L0)));
     big = fabsf(step) * 1.2e-7f > tol;
+    dstep = fabsf(step);
     // corrections far below the convergence tolerance are dropped (bitwise fixed point, tiles lock)
     return fabsf(step) <= tol ? L0 : L0 + widen_exact(step);
 }
@@ -138,17 +140,20 @@ __device__ __forceinline__ double adj2_polish(double T0, double Txp, double Txm,
 // (FP64 differences and residual, 8 FP64 instructions; FP32 derivative and step); a: x-neighbour
 // minimum, b: z-neighbour minimum.  big: the step's second-order remainder exceeds the floor.
 __device__ __forceinline__ double eik2_newton(double U0, double a, double b, double s, double dx, double dz, double wx,
-                                              double wz, float wxf, float wzf, float floor, bool& big) {
+                                              double wz, float wxf, float wzf, float floor, bool& big,
+                                              float& dstep) {
     const double px = pos_sign(U0 - a), pz = pos_sign(U0 - b);
     const double f = fma(wx * px, px, fma(wz * pz, pz, -s * s));
     const float fp = 2.0f * (wxf * narrow_trunc(px) + wzf * narrow_trunc(pz));
     if (!(fp > 0.0f)) {
         big = true;
+        dstep = INFINITY;   // a restart: the change is not a Newton step
         return fmin(fma(dx, s, a), fma(dz, s, b));
     }
     const float step = __fdividef(narrow_trunc(f), fp);
     const float sw = (dbits(px) > 0 ? wxf : 0.0f) + (dbits(pz) > 0 ? wzf : 0.0f);
     big = sw * step * step > floor * fp;
+    dstep = fabsf(step);   // the change of the node, to FP32 precision
     return fabsf(step) <= floor ? U0 : U0 - widen_exact(step);   // bitwise fixed point once converged
 }
 
@@ -284,8 +289,15 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     const int omask = kSelective ? (dm >> 4) & 0xf : 0xf;
     if (!(dm & omask & obit)) return;   // locked for this order (warp-uniform)
     __syncwarp();
+    // Convergence test of the mixed kinds (FP32 bulk, polish): a node that moved by more than
+    // the tolerance in some processing of this outer iteration, ORed over the iteration (a
+    // polish change is its FP32 step).  The plain kinds compare with a snapshot taken at the
+    // tile's first processing in the iteration, as the reference's isconv does.
+    constexpr bool kSnap = KIND == kFwdPlain64 || KIND == kAdjPlain64;
+    // the tile's lock word as lane 0 last wrote it (no other tile of this launch writes it)
+    int dword = kSelective ? (dm & ~obit) : 0;
     if (lane == 0) {
-        dirty[tid] = kSelective ? (dm & ~obit) : 0;
+        dirty[tid] = dword;
         if (A.work) atomicAdd(A.work + q, (unsigned long long)(min(T2I, A.nr - ti * T2I) * min(T2J, A.nc - tj * T2J)));
     }
     const int i0 = ti * T2I, j0 = tj * T2J;
@@ -296,7 +308,7 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     Real* box = reinterpret_cast<Real*>(smem_raw + warp * warp_smem2<KIND>());
     Aux* tbox = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + H2I * R2 * sizeof(Real));
     Real* fld = reinterpret_cast<Real*>(A.field) + A.inst_off[q];
-    Real* snp = reinterpret_cast<Real*>(A.snap) + q * n;
+    Real* snp = kSnap ? reinterpret_cast<Real*>(A.snap) + q * n : nullptr;
 
     const Real fill = ADJ ? Real(0) : Real(INFINITY);
     load_box2(box, fld, i0, j0, nr, nc, fill, lane, Ident2());
@@ -323,14 +335,26 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
         }
     }
 
-    // snapshot at the tile's first processing in this outer iteration
-    int* stamp = A.stamp + (long long)q * A.ntiles;
-    if (__ldcg(stamp + tid) != iter) {
-        for (int y = 0; y < ei; ++y)
-            for (int x = lane; x < ej; x += 32) snp[(long long)(i0 + y) * nc + j0 + x] = box[(y + 1) * R2 + x + 1];
-        if (lane == 0) stamp[tid] = iter;
+    // snapshot at the tile's first processing in this outer iteration (plain kinds)
+    if constexpr (kSnap) {
+        int* stamp = A.stamp + (long long)q * A.ntiles;
+        if (__ldcg(stamp + tid) != iter) {
+            for (int y = 0; y < ei; ++y)
+                for (int x = lane; x < ej; x += 32) snp[(long long)(i0 + y) * nc + j0 + x] = box[(y + 1) * R2 + x + 1];
+            if (lane == 0) stamp[tid] = iter;
+        }
     }
     __syncwarp();
+    bool moved = false;
+    const float tabs_f = narrow_trunc(A.tol_abs), trel_f = narrow_trunc(A.tol_rel);   // FP32 kinds' test
+    // the mixed kinds' test at a changed node (old -> nv; dstep: the polish step's size)
+    auto note_move = [&](Real old, Real nv, float dstep) {
+        if constexpr (kSelective) {
+            if (dstep > tabs_f) moved = true;
+        } else if constexpr (!kSnap) {
+            if (fabsf(old - nv) > tabs_f + trel_f * fabsf(nv)) moved = true;
+        }
+    };
 
     int lim_row = -1, si = -1, sj = -1;
     if (A.inst_lim[q] >= 0) lim_row = A.inst_lim[q];
@@ -402,6 +426,7 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                 if (upd) {
                     const Real old = box[c];
                     Real nv = old;
+                    float dstep = INFINITY;   // polish: the size of this node's change
                     const Real bz = ref_min(box[c - R2], box[c + R2]);
                     const Real ax = ref_min(box[c + 1], box[c - 1]);
                     const Real s = __ldg(slow + (long long)gi * nc + gj);
@@ -418,13 +443,14 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         if (m & obit) {
                             bool big = false;
                             nv = eik2_newton(old, ax, bz, s, A.dx, A.dz, A.inv2x, A.inv2z, A.wxf, A.wzf,
-                                             A.polish_floor, big);
+                                             A.polish_floor, big, dstep);
                             restep |= big;
                         }
                     }
                     if (!bits_same(old, nv)) {
                         box[c] = nv;
                         chg = true;
+                        note_move(old, nv, dstep);
                         if constexpr (kPrune) {
                             auto dep = [&](int n) { return min(obits2(old), obits2(nv)) < obits2(box[n]); };
                             if (li == 0 && dep(c - R2)) m_ilo = true;
@@ -446,6 +472,7 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                 if (row_interior && gj >= 1 && gj <= nc - 2 && !(fb & 1u)) {
                     const Real old = box[c];
                     Real r = old;
+                    float dstep = INFINITY;   // polish: the size of this node's change
                     if constexpr (!TWIN2) {   // FP32 bulk: from the staged offsets
                         T0 = tbox[c]; Txp = tbox[c + 1]; Txm = tbox[c - 1]; Tzp = tbox[c + R2]; Tzm = tbox[c - R2];
                     }
@@ -460,13 +487,14 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
                         if (m & obit) {
                             bool big = false;
                             r = adj2_polish(T0, Txp, Txm, Tzp, Tzm, box[c + 1], box[c - 1], box[c + R2], box[c - R2],
-                                            old, A.inv2x, A.inv2z, A.wxf, A.wzf, A.polish_floor, big);
+                                            old, A.inv2x, A.inv2z, A.wxf, A.wzf, A.polish_floor, big, dstep);
                             restep |= big;
                         }
                     }
                     if (!bits_same(old, r)) {
                         box[c] = r;
                         chg = true;
+                        note_move(old, r, dstep);
                         if constexpr (kPrune) {
                             // lambda at the neighbour node reads this node if its traveltime is larger
                             // (FP32 bulk: offsets from the tile's corner, compared as values)
@@ -500,7 +528,8 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
 
     if constexpr (kSelective) {
         const unsigned tsel = __reduce_or_sync(0xffffffffu, sel);
-        if (lane == 0) dirty[tid] = (dirty[tid] & 0xf) | (int)(tsel << 4);
+        dword = (dword & 0xf) | (int)(tsel << 4);
+        if (lane == 0) dirty[tid] = dword;
     }
     // nothing changed: field and snapshot comparison stand as they are
     if (!__any_sync(0xffffffffu, chg)) return;
@@ -516,28 +545,27 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
     if constexpr (kSelective) again = __any_sync(0xffffffffu, restep);
     else if constexpr (kPrune) again = __any_sync(0xffffffffu, stale);
     if (lane == 0) {
-        dirty[tid] |= again ? 0xf : (kSelective ? (0xf & ~obit) : 0);
+        dirty[tid] = dword | (again ? 0xf : (kSelective ? (0xf & ~obit) : 0));
         if (f_ilo && ti > 0) atomicOr(dirty + tid - A.nbj, 0xf);
         if (f_ihi && ti < A.nbi - 1) atomicOr(dirty + tid + A.nbj, 0xf);
         if (f_jlo && tj > 0) atomicOr(dirty + tid - 1, 0xf);
         if (f_jhi && tj < A.nbj - 1) atomicOr(dirty + tid + 1, 0xf);
     }
-    bool moved = false;
-    const float tabs_f = narrow_trunc(A.tol_abs), trel_f = narrow_trunc(A.tol_rel);   // FP32 kinds' test
     for (int y = 0; y < ei; ++y) {
         for (int x = lane; x < ej; x += 32) {
             const long long at = (long long)(i0 + y) * nc + j0 + x;
             const Real v = box[(y + 1) * R2 + x + 1];
             fld[at] = v;
-            if constexpr (sizeof(Real) == 8) {
+            if constexpr (kSnap)
                 if (fabs(__ldcg(snp + at) - v) > A.tol_abs + A.tol_rel * fabs(v)) moved = true;   // isconv
-            } else {
-                if (fabsf(__ldcg(snp + at) - v) > tabs_f + trel_f * fabsf(v)) moved = true;
-            }
         }
     }
     const bool any_moved = __any_sync(0xffffffffu, moved);
-    if (lane == 0) A.diff[(long long)q * A.ntiles + tid] = any_moved ? 1 : 0;
+    if constexpr (kSnap) {
+        if (lane == 0) A.diff[(long long)q * A.ntiles + tid] = any_moved ? 1 : 0;
+    } else {
+        if (lane == 0 && any_moved) A.diff[(long long)q * A.ntiles + tid] = 1;
+    }
 }
 
 template <int KIND>
