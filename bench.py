@@ -328,7 +328,7 @@ def main():
     # ratio of measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum over the
     # 1680 launches of the phase, 9-source case of this grid) to the algorithmic bytes of the
     # same launches.  The excess over 1 is the halo re-read.
-    traffic_ratio = {"fwd64": 1.14, "adj64": 1.89}
+    traffic_ratio = {"fwd64": 1.09, "adj64": 1.89}
     traffic = (alg_bytes / launches_dom * traffic_ratio[dom]) if (dom in traffic_ratio and launches_dom) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_unit": "bytes per launch",
