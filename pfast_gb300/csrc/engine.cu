@@ -2,11 +2,12 @@
 // outer-iteration driver, the 3D pipelines and the C ABI.
 //
 // The per-source loops of the reference drivers (src/T_PFAST3D.cpp:387-399,
-// 672-686) become batches of sources on one GPU.  Every solve keeps the
+// 672-686) become batches of sources on one GPU.  The plain solves keep the
 // reference's outer-iteration semantics: an iteration = snapshot + 2^d ordered
 // sweeps, repeated while some node moved by more than 1e-9 and fewer than MAXSwp
-// iterations ran (src/T_pfsm3d.h:152, src/T_padjoint3d.h:135).  Converged sources
-// retire from the batch; the others keep sweeping.
+// iterations ran (src/T_pfsm3d.h:152, src/T_padjoint3d.h:135).  The mixed phases
+// repeat while some processing of the iteration moved a node by more than their
+// tolerance.  Converged sources retire from the batch; the others keep sweeping.
 
 #include <cstdarg>
 #include <cstdio>

@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(kWarps2 * 32) sweep2d_kernel(const Sweep2Args 
         dword = (dword & 0xf) | (int)(tsel << 4);
         if (lane == 0) dirty[tid] = dword;
     }
-    // nothing changed: field and snapshot comparison stand as they are
+    // nothing changed: the field and its convergence flag stand as they are
     if (!__any_sync(0xffffffffu, chg)) return;
     // unlock this tile and the face neighbours that see a changed face node (lane = row)
     const unsigned f_ilo = __ballot_sync(0xffffffffu, kPrune ? m_ilo : chg && li == 0);

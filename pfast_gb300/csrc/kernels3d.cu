@@ -373,11 +373,13 @@ __device__ __forceinline__ long long obits(float x) { return __float_as_int(x); 
 //             or for the FP32 bulk and the adjoint polish the tiles with something to
 //             propagate), and for all eight orders by a face neighbour whose changed face
 //             node the tile reads, or by the tile itself (see process_tile),
-//   stamp[t]  outer iteration in which the tile last took its snapshot,
-//   diff[t]   whether the tile differs from its snapshot by more than the
-//             tolerance after its latest processing (cleared each iteration).
-// The outer-iteration test of the reference (isconv) is the OR of diff over the
-// tiles of a source: a skipped tile has not moved.
+//   stamp[t]  outer iteration in which the tile last took its snapshot (plain kinds),
+//   diff[t]   plain kinds: whether the tile differs from its snapshot by more than the
+//             tolerance after its latest processing; mixed kinds: whether some processing
+//             in this iteration moved a node by more than the tolerance (cleared each
+//             iteration).
+// The outer-iteration test (the reference's isconv for the plain kinds) is the OR of diff
+// over the tiles of a source: a skipped tile has not moved.
 // Tile (tk, ti, tj) and its index of the diagonal-table entry pk in sweep order dir (the
 // table is in flipped coordinates).
 __device__ __forceinline__ int tile_of(const Sweep3Args& A, unsigned pk, int dir, int& tk, int& ti, int& tj) {
