@@ -215,7 +215,7 @@ static pfast_status iteration_graph(pfast_ctx* ctx, const Sweep3Args& a, int kin
     cudaError_t e = cudaMemsetAsync(k.diff, 0, sizeof(int) * (size_t)k.ntiles * nb, st);
     for (int dir = 0; dir < 8 && !r && e == cudaSuccess; ++dir) {
         k.dir = dir;
-        for (int d = 0; d < dt.ndiag && !r; ++d) r = launch_sweep3(kind, k, d, dt.h_off[d + 1] - dt.h_off[d], nact, st);
+        for (int d = 0; d < dt.ndiag && !r; ++d) r = launch_sweep3(kind, k, dt.h_off[d], dt.h_off[d + 1] - dt.h_off[d], nact, st);
     }
     if (!r && e == cudaSuccess) e = cudaMemsetAsync(k.changed, 0, sizeof(int) * nb, st);
     if (!r && e == cudaSuccess)
@@ -341,7 +341,7 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
             for (int dir = 0; dir < 8; ++dir) {
                 a.dir = dir;
                 for (int d = 0; d < dt.ndiag; ++d) {
-                    PFAST_LAUNCH(ctx, launch_sweep3(kind, a, d, dt.h_off[d + 1] - dt.h_off[d], nact, st));
+                    PFAST_LAUNCH(ctx, launch_sweep3(kind, a, dt.h_off[d], dt.h_off[d + 1] - dt.h_off[d], nact, st));
                 }
             }
             PFAST_CUDA_TRY(cudaMemsetAsync(a.changed, 0, sizeof(int) * nb, st));

@@ -756,20 +756,24 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
 // One launch per tile diagonal: block (x, y) = (tile of the diagonal, active instance).
 template <int KIND>
-__global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args A, const int d) {
+// d0, ntd: the diagonal's first entry in diag_tiles and its tile count.
+__global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args A, const int d0, const int ntd) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int d0 = A.diag_off[d];
     const int tile_idx = blockIdx.x * kWarps3 + warp;
-    if (tile_idx >= A.diag_off[d + 1] - d0) return;
-    int iter = A.iter;
-    if (A.dyn) {   // replayed iteration graph
-        if ((int)blockIdx.y >= __ldcg(A.dyn + 1)) return;
-        iter = __ldcg(A.dyn);
-    }
+    if (tile_idx >= ntd) return;
+    // Three independent reads, issued before any is tested, so that a locked tile costs two
+    // memory round trips (these, then its lock word): the iteration and active count of a
+    // replayed iteration graph, the instance of this block row (act holds at least gridDim.y
+    // entries) and the tile of this diagonal entry.
+    int2 dyn = make_int2(A.iter, (int)gridDim.y);
+    if (A.dyn) dyn = __ldcg(reinterpret_cast<const int2*>(A.dyn));
     const int inst = A.act[blockIdx.y];
+    const unsigned pk = A.diag_tiles[d0 + tile_idx];
+    if ((int)blockIdx.y >= dyn.y) return;   // a source retired since the graph was captured
+    const int iter = dyn.x;
     int tk, ti, tj;
-    const int tid = tile_of(A, A.diag_tiles[d0 + tile_idx], A.dir, tk, ti, tj);
+    const int tid = tile_of(A, pk, A.dir, tk, ti, tj);
     const int dm = __ldcg(A.dirty + (long long)inst * A.ntiles + tid);
     if (!tile_due<KIND>(dm, A.dir)) return;   // locked tile for this order (warp-uniform)
     __syncwarp();
@@ -1007,7 +1011,7 @@ size_t sweep3_smem_bytes(int kind) {
 }
 
 template <int KIND>
-static pfast_status launch_one(const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st) {
+static pfast_status launch_one(const Sweep3Args& a, int d0, int tiles, int nact, cudaStream_t st) {
     static bool attr_set = false;
     const size_t smem = (size_t)kWarps3 * warp_smem_bytes<KIND>();
     if (!attr_set) {
@@ -1015,7 +1019,7 @@ static pfast_status launch_one(const Sweep3Args& a, int d, int tiles, int nact, 
         attr_set = true;
     }
     dim3 grid((tiles + kWarps3 - 1) / kWarps3, nact);
-    sweep3d_kernel<KIND><<<grid, kWarps3 * 32, smem, st>>>(a, d);
+    sweep3d_kernel<KIND><<<grid, kWarps3 * 32, smem, st>>>(a, d0, tiles);
     return PFAST_OK;
 }
 
@@ -1147,15 +1151,15 @@ pfast_status launch_reduce_diff(const int* diff, const int* dirty, bool selectiv
     return PFAST_OK;
 }
 
-pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d, int tiles, int nact, cudaStream_t st) {
+pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d0, int tiles, int nact, cudaStream_t st) {
     if (tiles <= 0 || nact <= 0) return PFAST_OK;
     switch (kind) {
-        case kFwdPlain64: return launch_one<kFwdPlain64>(a, d, tiles, nact, st);
-        case kFwdFast32: return launch_one<kFwdFast32>(a, d, tiles, nact, st);
-        case kFwdPolish64: return launch_one<kFwdPolish64>(a, d, tiles, nact, st);
-        case kAdjPlain64: return launch_one<kAdjPlain64>(a, d, tiles, nact, st);
-        case kAdjFast32: return launch_one<kAdjFast32>(a, d, tiles, nact, st);
-        case kAdjPolish64: return launch_one<kAdjPolish64>(a, d, tiles, nact, st);
+        case kFwdPlain64: return launch_one<kFwdPlain64>(a, d0, tiles, nact, st);
+        case kFwdFast32: return launch_one<kFwdFast32>(a, d0, tiles, nact, st);
+        case kFwdPolish64: return launch_one<kFwdPolish64>(a, d0, tiles, nact, st);
+        case kAdjPlain64: return launch_one<kAdjPlain64>(a, d0, tiles, nact, st);
+        case kAdjFast32: return launch_one<kAdjFast32>(a, d0, tiles, nact, st);
+        case kAdjPolish64: return launch_one<kAdjPolish64>(a, d0, tiles, nact, st);
     }
     set_last_error("unknown sweep kind %d", kind);
     return PFAST_ERR_INVALID;

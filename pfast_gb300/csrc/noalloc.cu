@@ -193,7 +193,7 @@ extern "C" pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src
         for (int dir = 0; dir < 8; ++dir) {
             a.dir = dir;
             for (int d = 0; d < ndiag; ++d) {
-                r = launch_sweep3(kFwdPlain64, a, d, off[d + 1] - off[d], 1, s);
+                r = launch_sweep3(kFwdPlain64, a, off[d], off[d + 1] - off[d], 1, s);
                 if (r) return r;
             }
         }
