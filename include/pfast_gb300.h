@@ -352,15 +352,19 @@ pfast_status pfast_server_stats_get(pfast_server* srv, pfast_server_stats* st);
 /* ------------------------------------------------------- no-allocation entry point
  * No counterpart in the reference.  The traveltime field of one point source --
  * the computation of pfast_fsm3d (plain FP64, bit-identical to it) -- for callers
- * that cannot allocate device memory: code running under CUDA stream capture, or
- * inside a host whose own allocator or memory budget owns the device.  vp and U are
- * DEVICE arrays [nz*nrows*ncols] owned by the caller; `stream` is a cudaStream_t
- * (NULL: the default stream).  The call makes no cudaMalloc / cudaFree: its work
- * memory is one static device array sized for PFAST_NOALLOC_MAX_NODES grid nodes
- * (about 16.1 MiB, held by every GPU that loads the library until the process
- * exits).  Larger grids are rejected with PFAST_ERR_INVALID.  The first call on a
- * device looks the array up (cudaGetSymbolAddress) and should come before any
- * stream capture.  All calls share the array: calls that overlap on the GPU race.
+ * that cannot allocate device memory: a host whose own pool allocator or memory
+ * budget owns the device and forbids libraries to allocate, or a loop that must not
+ * meet the allocator's synchronisation.  vp and U are DEVICE arrays
+ * [nz*nrows*ncols] owned by the caller; `stream` is a cudaStream_t (NULL: the
+ * default stream).  The call makes no cudaMalloc / cudaFree: its work memory is one
+ * static device array sized for PFAST_NOALLOC_MAX_NODES grid nodes (about 16.1 MiB,
+ * held by every GPU that loads the library until the process exits).  Larger grids
+ * are rejected with PFAST_ERR_INVALID.  The first call on a device looks the array
+ * up (cudaGetSymbolAddress) and caches its address; make that first call before any
+ * stream capture, and do not reuse the library across cudaDeviceReset.  The call
+ * blocks the calling thread: it synchronises `stream` after the velocity check and
+ * once per outer iteration to read the convergence flag.  All calls share the
+ * array: calls that overlap on the GPU race.
  */
 #define PFAST_NOALLOC_MAX_NODES 1048576
 pfast_status pfast_fsm3d_noalloc(const double* vp, double* U, int src_row, int src_col, int src_z, int MAXSwp,

@@ -1,5 +1,5 @@
 """Build recipe for oracle/_ref: the reference's own hot-path headers, compiled
-from where they lie (REF_ROOT/src, default /root/reference/src), wrapped by
+from where they lie (<reference tree>/src), wrapped by
 oracle/ref_harness{2d,3d}.cpp.  Test infrastructure only.
 
 Compiled with g++ -O2 -ffp-contract=off (FMA contraction off, the setting under
@@ -19,7 +19,8 @@ OUT = os.path.join(HERE, "_ref")
 
 
 def ref_root():
-    return os.environ.get("PFAST_REF_ROOT", "/root/reference")
+    """The reference tree: $PFAST_REF_ROOT, else a `reference` folder beside the checkout."""
+    return os.environ.get("PFAST_REF_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def build(verbose=False):

@@ -1,7 +1,7 @@
 """ctypes binding of libpfast_gb300.so (the C ABI declared in include/pfast_gb300.h).
 
-The library is the only compute path: if it has not been built this module
-raises at import, there is no CPU fallback.
+The library is the only compute path: lib() loads it on first use and raises if
+it has not been built; there is no CPU fallback.
 """
 import ctypes as C
 import os

@@ -74,6 +74,8 @@ pfast_status launch_polish_orders3(int kind, const Sweep3Args& a, int nb, int na
 // where the tile's halo box holds a reached traveltime / nonzero lambda, else 0.  Every kind but
 // the forward polish (whose starting field is reached everywhere): no-op for that one.
 pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStream_t st);
+// One tile-diagonal launch over grid (tiles, nact): a.act must hold at least nact entries
+// (every block reads a.act[blockIdx.y] before it tests whether its instance is still active).
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d0, int tiles, int nact, cudaStream_t st);
 // Persistent sweep kernel: `blocks` blocks of `warps` warps take the nact instances of a.act
 // from *queue (zeroed by the caller) and solve each to convergence (maxiter outer

@@ -1,24 +1,28 @@
 // noalloc.cu -- pfast_fsm3d_noalloc: the single-source first-arrival solve for
 // callers that cannot allocate device memory.
 //
-// Who needs it: code that runs where cudaMalloc is not allowed or not wanted --
-// for example inside a CUDA stream capture (an allocation call is not capturable
-// and would invalidate the capture), in a host that hands every device byte to
-// its own pool allocator or budget and forbids allocations by libraries, or in a
-// real-time loop that must not hit the allocator's synchronisation.  The caller
-// owns the model and the output on the device; every byte of work memory this
-// entry point needs comes from one file-scope static device array of fixed size,
-// which each GPU that loads the library holds until the process exits.
+// Who needs it: a host program whose own pool allocator or memory budget owns every
+// byte of the device and forbids libraries to call cudaMalloc (simulation frameworks
+// and game engines commonly do this), or a latency-bound loop that must not meet the
+// allocator's implicit synchronisation.  The caller owns the model and the output on
+// the device; every byte of work memory this entry point needs comes from one
+// file-scope static device array of fixed size, which each GPU that loads the library
+// holds until the process exits.
 //
 // The array holds, for at most PFAST_NOALLOC_MAX_NODES grid nodes: the slowness
 // field, the iteration-start snapshot, the tile-diagonal table, the per-tile
 // locking flags and a few words.
 // Its device address is taken with cudaGetSymbolAddress once per device, on the
-// first call made on that device (with that device current); that first call
-// should therefore come before any stream capture.  Every call shares the array
-// and it keeps the last call's contents: this file writes or clears everything it
-// reads before reading it, and calls that overlap on the GPU (on different streams
-// or host threads) race on it.
+// first call made on that device (with that device current), and cached for the
+// life of the process; that first call should come before any stream capture, and
+// the cached address is not valid after cudaDeviceReset (the module is loaded again,
+// possibly elsewhere).  Every call shares the array and it keeps the last call's
+// contents: this file writes or clears everything it reads before reading it, and
+// calls that overlap on the GPU (on different streams or host threads) race on it.
+//
+// The call blocks the calling thread: it reads a velocity-check flag and, once per
+// outer iteration, a convergence flag back to the host (synchronising `stream` each
+// time), because the number of iterations depends on the field.
 //
 // The sweeps are the library's plain FP64 kernels (bit-identical to pfast_fsm3d).
 

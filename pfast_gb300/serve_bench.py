@@ -125,7 +125,7 @@ def run_stream(srv, pool3, pool2, rate, duration, precision, rng, max_inflight=2
             info, ok = {}, False
         t_done = time.perf_counter()
         with lock:
-            records.append(dict(dim=plan["dim"], kind=plan["kind"], nsrc=plan["nsrc"], ok=ok,
+            records.append(dict(dim=plan["dim"], kind=plan["kind"], nsrc=plan["nsrc"], ok=ok, lag_ms=plan["lag_ms"],
                                 latency_ms=(t_done - t_arr) * 1e3, queue_ms=info.get("queue_ms", 0.0),
                                 run_ms=info.get("run_ms", 0.0), t_done=t_done))
         srv.drop_survey(plan["sid"])
@@ -139,6 +139,7 @@ def run_stream(srv, pool3, pool2, rate, duration, precision, rng, max_inflight=2
             time.sleep(delay)
         sem.acquire()
         t_arr = time.perf_counter()
+        plan["lag_ms"] = (t_arr - t0 - plan["t"]) * 1e3   # > 0: the client offered it late
         prng = np.random.default_rng(plan["seed"])
         shape = plan["vp"].shape
         if plan["mid"] not in done_models:
@@ -176,7 +177,20 @@ def summarize(records, wall_s, rate):
     return {"offered_rate": rate, "requests": len(records), "failed": len(records) - len(ok),
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_queue_ms": float(np.mean([r["queue_ms"] for r in ok])) if ok else 0.0,
-            "requests_per_s": len(ok) / wall_s, "solves_per_s": solves / wall_s, "wall_s": wall_s}
+            "requests_per_s": len(ok) / wall_s, "solves_per_s": solves / wall_s, "wall_s": wall_s,
+            "arrival_lag_ms_p99": float(np.percentile([r["lag_ms"] for r in records], 99)) if records else 0.0}
+
+
+def knee(results, factor=2.0):
+    """The lowest offered rate at which p99 latency exceeds `factor` times the p99 at the lowest
+    rate, or the completed requests fall below 90% of the offered rate (None: not reached)."""
+    if not results:
+        return None
+    base = results[0]["p99_ms"]
+    for r in results:
+        if r["p99_ms"] > factor * base or r["requests_per_s"] < 0.9 * r["offered_rate"]:
+            return r["offered_rate"]
+    return None
 
 
 def sweep(rates, duration, precision, slots=8, budget_gb=150.0, seed=5, pool=None):

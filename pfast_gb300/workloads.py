@@ -42,9 +42,10 @@ def main():
     p.add_argument("--sources", type=int, default=16, help="number of sources (a square number)")
     p.add_argument("--precision", choices=["plain", "mixed"], default="mixed")
     p.add_argument("--evals", type=int, default=1)
-    p.add_argument("--picks-precision", choices=["plain", "mixed"], default="mixed",
-                   help="solver of the observed picks (plain: the evaluation is the only user of the mixed kernels)")
-    p.add_argument("--no-graphs", action="store_true", help="launch the sweeps one by one (kernel indices for ncu -s)")
+    p.add_argument("--picks-precision", choices=["plain", "mixed"], default="plain",
+                   help="solver of the observed picks on the true model (plain FP64 by default)")
+    p.add_argument("--no-graphs", action="store_true",
+                   help="launch each outer iteration's sweeps one by one instead of replaying captured graphs")
     a = p.parse_args()
     side = int(round(np.sqrt(a.sources)))
     nz, nr, nc = a.grid

@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 from oracle import build_ref, ref  # noqa: E402
 from pfast_gb300 import io as pio  # noqa: E402   (pure numpy helpers; no CUDA needed)
 
-REF = os.environ.get("PFAST_REF_ROOT", "/root/reference")
+REF = build_ref.ref_root()
 M = os.path.join(REF, "models")
 SRC_SUBSET = np.arange(0, 56, 4)
 

@@ -2,6 +2,7 @@
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -93,3 +94,17 @@ def test_synthetic_generators_are_seeded():
     vt, v0, Z = synth.joint2d_models()
     assert vt.shape == (201, 601) and Z.shape == (601, 3)
     assert np.all(Z[:, 1] < 0)
+
+
+def test_workload_generators_load_no_cuda_library():
+    """bench.py's reference arm imports the seeded generators; they must not map
+    libpfast_gb300.so (the reference arm runs the CPU restatement only)."""
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "import pfast_gb300\n"
+            "from pfast_gb300 import synth, workloads, _capi\n"
+            "workloads.c3_inputs(8, 16, 16, 2, 4)\n"
+            "assert _capi._lib is None\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libpfast_gb300' not in maps\n" % ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]

@@ -72,7 +72,9 @@ def test_pins3d_fields_and_misfit_match_reference():
             assert float(E).hex() == want["EE_hex"]
 
 
-REF_TREE = os.environ.get("PFAST_REF_ROOT", "/root/reference")
+from oracle.build_ref import ref_root  # noqa: E402
+
+REF_TREE = ref_root()
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF_TREE, "models")), reason="reference tree not present")
