@@ -50,11 +50,13 @@ typedef struct {
                              (adjoint: times 1 + |lambda|) are dropped, so converged regions reach
                              a bitwise fixed point; 0 = the default, 1e-10.  Keep it well below the
                              1e-9 convergence tolerance. */
-    int schedule;         /* 3D sweeps: 0 = automatic (the faster one measured by pfast_survey3d_autotune
-                             for this grid shape and source count; untuned: persistent from 4 sources
-                             per SM), 1 = one launch per tile diagonal (every tile of every source
-                             spread over all SMs), 2 = persistent (one block solves one source).
-                             Same results. */
+    int schedule;         /* 3D sweeps: 0 = automatic (per sweep kind, the faster one measured by
+                             pfast_survey3d_autotune for this grid shape and source count; untuned:
+                             persistent from 2 sources per SM), 1 = one launch per tile diagonal
+                             (every tile of every source spread over all SMs), 2 = persistent: one
+                             dataflow launch per phase, one block solves one source with its sweep
+                             orders overlapping as the tile dependencies allow (grids of at most
+                             8192 tiles of 4x8x32 nodes; larger grids use 1).  Same results. */
     int near_source_radius;  /* 3D forward, opt-in (not in the reference): nodes within this many grid
                              nodes of the source (Euclidean, in nodes) start from the straight-ray
                              traveltime 0.5*(s_src + s_node)*distance and stay fixed, which removes most

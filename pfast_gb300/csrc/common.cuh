@@ -33,7 +33,7 @@ static_assert(PS >= HI * HJ && (PS - 1) % 32 == 8 && (HJ - 1) % 32 == 1, "bank-c
 constexpr int SJ = TJ + 2, SPS = 297;
 static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
 // Warps (tiles) per CTA.
-constexpr int kMaxPWarps = 16;   // warps per block of the persistent sweep kernel, at most
+constexpr int kDataflowMaxTiles = 8192;   // tiles per instance the dataflow kernel keeps in shared memory
 constexpr int kWarps3 = 1;   // one-warp CTAs: the finest shared-memory granularity, hence the most warps per SM
 
 // ---------------------------------------------------------------- 2D tiles

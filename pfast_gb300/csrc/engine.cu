@@ -160,7 +160,7 @@ Spacing3 make_spacing(double dx, double dy, double dz) {
 // Schedule autotuner, per (device, sweep kind, grid, active instances): phase times of the two
 // schedules measured by pfast_survey3d_autotune, which runs the same evaluation once with each
 // (identical inputs, identical bits).  An automatic phase uses the faster one once both are
-// known; before that, the persistent kernel from 4 instances per SM, else one launch per tile
+// known; before that, the dataflow kernel from two instances per SM, else one launch per tile
 // diagonal.
 struct TuneEntry {
     double ms[2] = {0.0, 0.0};
@@ -174,7 +174,7 @@ static int tuned_schedule(const std::tuple<int, int, int, int, int, int>& key, i
     auto it = g_tune.find(key);
     if (it != g_tune.end() && it->second.n[0] > 0 && it->second.n[1] > 0)
         return it->second.ms[1] / it->second.n[1] < it->second.ms[0] / it->second.n[0] ? 1 : 0;
-    return std::get<5>(key) >= 4 * sms ? 1 : 0;
+    return std::get<5>(key) >= 2 * sms ? 1 : 0;
 }
 
 static void tune_record(const std::tuple<int, int, int, int, int, int>& key, int which, double ms) {
@@ -284,29 +284,37 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
         if (polish) PFAST_LAUNCH(ctx, launch_polish_orders3(kind, a, nb, nact0, st));
     }
     // Two schedules.  Per-diagonal launches spread every tile of every active instance over
-    // all SMs (one warp per tile) and suit surveys with few instances per SM, such as 256
-    // sources on 152 SMs; the persistent kernel (one block solves one instance, no host
-    // round trip per iteration) suits runs with several instances per SM.  Automatic: the
-    // autotuner above.
+    // all SMs (one warp per tile) and suit surveys with few instances; the dataflow kernel
+    // (one block solves one instance, its sweep orders overlapping as their tile dependencies
+    // allow, no host round trip per iteration) suits runs with about one instance per SM or
+    // more.  Automatic: the autotuner above.  Grids whose tiles do not fit the dataflow
+    // kernel's shared memory use the per-diagonal launches.
     int dev = 0, sms = 1;
     PFAST_CUDA_TRY(cudaGetDevice(&dev));
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const auto tkey = std::make_tuple(dev, kind, a.nz, a.nr, a.nc, (int)active.size());
-    const bool persistent = ctx->schedule == PFAST_SCHEDULE_PERSISTENT ||
-                            (ctx->schedule == PFAST_SCHEDULE_AUTO && !active.empty() && tuned_schedule(tkey, sms) == 1);
+    int dwarps = 0, dblocks = 0;
+    if (!active.empty()) PFAST_TRY(dataflow_shape(kind, a.ntiles, (int)active.size(), &dwarps, &dblocks));
+    const bool persistent = dwarps > 0 &&
+                            (ctx->schedule == PFAST_SCHEDULE_PERSISTENT ||
+                             (ctx->schedule == PFAST_SCHEDULE_AUTO && tuned_schedule(tkey, sms) == 1));
     if (persistent && maxiter > 0) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
-        PFAST_TRY(ctx->queue.ensure(sizeof(int)));
-        PFAST_CUDA_TRY(cudaMemsetAsync(ctx->queue.p, 0, sizeof(int), st));
-        a.ndiag = dt.ndiag;
-        int warps = 1, blocks = 1;
-        PFAST_TRY(persistent_shape(kind, nact, &warps, &blocks));
-        PFAST_TRY(launch_sweep3_persistent(kind, a, nact, maxiter, ctx->queue.as<int>(), a.changed, warps, blocks, st));
+        PFAST_TRY(ctx->queue.ensure(2 * sizeof(int)));
+        PFAST_CUDA_TRY(cudaMemsetAsync(ctx->queue.p, 0, 2 * sizeof(int), st));
+        PFAST_TRY(launch_sweep3_dataflow(kind, a, nact, maxiter, ctx->queue.as<int>(), a.changed, dwarps, dblocks, st));
         ++ctx->launches;
+        PFAST_TRY(ctx->h_dyn.ensure(2 * sizeof(int)));
+        int* hq = ctx->h_dyn.as<int>();
+        PFAST_CUDA_TRY(cudaMemcpyAsync(hq, ctx->queue.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
         PFAST_CUDA_TRY(cudaMemcpyAsync(h_chg, a.changed, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
         PFAST_CUDA_TRY(cudaStreamSynchronize(st));
+        if (hq[1]) {
+            set_last_error("dataflow sweep: a block made no progress for two seconds (internal error)");
+            return PFAST_ERR_CUDA;
+        }
         std::vector<int> still;
         for (int id : active) {
             iters[id] = h_chg[id] & 0xffff;

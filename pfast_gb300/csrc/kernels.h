@@ -29,7 +29,6 @@ struct Sweep3Args {
     const unsigned* diag_tiles;  //   diag_tiles[diag_off[d] .. diag_off[d+1])
     int nz, nr, nc;
     int nbk, nbi, nbj;
-    int ndiag;                // tile diagonals (persistent kernel)
     Spacing3 sp;
     int dir;                  // sweep order 0..7: bit2 = s3>0 (z), bit1 = s1>0 (rows), bit0 = s2>0 (cols)
     int iter;                 // outer-iteration index (snapshot stamps)
@@ -77,14 +76,16 @@ pfast_status launch_seed_tiles3(int kind, const Sweep3Args& a, int nact, cudaStr
 // One tile-diagonal launch over grid (tiles, nact): a.act must hold at least nact entries
 // (every block reads a.act[blockIdx.y] before it tests whether its instance is still active).
 pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d0, int tiles, int nact, cudaStream_t st);
-// Persistent sweep kernel: `blocks` blocks of `warps` warps take the nact instances of a.act
-// from *queue (zeroed by the caller) and solve each to convergence (maxiter outer
-// iterations at most); result[inst] = iterations | 1<<30 if not converged.
-pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
-                                      int warps, int blocks, cudaStream_t st);
-// Warps per block and resident blocks for the persistent kernel: the most warps per block
-// that still let every SM hold ceil(nact / SMs) blocks.
-pfast_status persistent_shape(int kind, int nact, int* warps, int* blocks);
+// Dataflow sweep kernel (one launch per phase): `blocks` blocks of `warps` warps take the
+// nact instances of a.act from queue[0] (zeroed by the caller) and solve each to convergence
+// (maxiter outer iterations at most); result[inst] = iterations | 1<<30 if not converged
+// (| 1<<29 and queue[1] |= 1 if a block stalled: an internal error).  a.dirty, a.diff,
+// a.stamp as for the per-diagonal launches; a.ntiles <= kDataflowMaxTiles.
+pfast_status launch_sweep3_dataflow(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
+                                    int warps, int blocks, cudaStream_t st);
+// Warps per block (as many as shared memory holds) and resident blocks
+// of the dataflow kernel; *warps = 0 when a grid of ntiles tiles does not fit.
+pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks);
 
 // Small 3D kernels.
 // s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64*sq_scale (if non-null); *bad is set

@@ -18,11 +18,13 @@
 // lanes per clock per SM on this part) go only where the precision is needed.
 
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <vector>
 #include <algorithm>
 #include <type_traits>
 #include "kernels.h"
+#include "dataflow3.h"
 
 namespace pfast {
 
@@ -781,77 +783,236 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
                               lane);
 }
 
-// Persistent form: one launch per phase.  Each block takes instances (sources) from a
-// queue and runs the whole solve of one instance -- outer iterations of eight ordered
-// sweeps until the instance's convergence test passes or maxiter iterations ran -- with
-// the tile diagonals of a sweep separated by block barriers (all tiles of an instance
-// are processed by the one block, so the diagonal order needs no other synchronisation).
-// Per diagonal, the block reads the lock words of up to blockDim tiles at once, lists
-// the tiles due in shared memory, and its warps process the list.
-// result[inst] = iterations run, | 1<<30 when maxiter stopped the solve unconverged.
+// ----------------------------------------------------------- dataflow schedule
+// One launch per phase.  Each block takes instances (sources) from a queue and runs the
+// whole solve of one instance: outer iterations of eight sweep orders until the instance's
+// convergence test passes or maxiter iterations ran.  Within an outer iteration the items
+// (sweep order o, tile x) form the dataflow graph of dataflow3.h: an item is ready once the
+// items it reads from are done, so the sweeps of different orders overlap and no barrier
+// separates tile diagonals or orders.  Per tile, two 4-bit counters in shared memory (one
+// per order parity, four tiles per word) count the item's missing dependencies; a ring of
+// ready items in shared memory feeds the block's warps.
+//   A warp takes about its share of the ready items (1 to 32, one per lane) and reads their
+//   lock words.  A tile that is not due in the item's order (tile locking) completes at once,
+//   lane by lane; of the due items the warp processes one (process_tile) and returns the
+//   others to the ring for idle warps.  Completing (o, x) re-arms x's counter of parity o for
+//   order o + 2 and decrements its dependents' counters; those that reach zero join the ring.
+//   The iteration ends when all 8 x ntiles items completed; the block then tests convergence
+//   as the per-diagonal schedule's reduction does (any tile moved / any tile still due).
+// Every tile processing sees exactly the neighbour values and lock words it sees in the
+// per-diagonal schedule, so both schedules give the same bits.  All waits are on this block's
+// own shared memory (no block waits for another) and are bounded: a block that sees no
+// progress for two seconds sets *err, records the instance as not converged and exits.
+// result[inst] = iterations | 1 << 30 when not converged.
+constexpr unsigned kSlotEmpty = 0xffffffffu;
+
+struct DataflowShared {
+    unsigned head, tail;   // ring positions: next to take / next to fill
+    int done;              // items completed in this outer iteration
+    int abort;
+    int item;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void df_push(unsigned* slots, unsigned qmask, DataflowShared* sh, unsigned e) {
+    const unsigned p = atomicAdd(&sh->tail, 1u);
+    unsigned* slot = slots + (p & qmask);
+    // a slot still holds an earlier round's item only while that item's taker is about to
+    // exchange it out (at most ntiles <= ring size items are outstanding): wait for it
+    for (int spin = 0; atomicCAS(slot, kSlotEmpty, e) != kSlotEmpty; ++spin)
+        if (spin > (1 << 22) || *(volatile int*)&sh->abort) { *(volatile int*)&sh->abort = 1; return; }
+}
+
+// One missing dependency of item (od, y) fewer; push it when it was the last.
+__device__ __forceinline__ void df_notify(unsigned* cnt, unsigned* slots, unsigned qmask, DataflowShared* sh, int y,
+                                          int od) {
+    const unsigned shf = 8u * (unsigned)(y & 3) + 4u * (unsigned)(od & 1);
+    const unsigned old = (atomicSub(cnt + (y >> 2), 1u << shf) >> shf) & 15u;
+    if (old == 1u) df_push(slots, qmask, sh, ((unsigned)y << 3) | (unsigned)od);
+    else if (old == 0u) *(volatile int*)&sh->abort = 1;   // more completions than dependencies: stop
+}
+
+// Completion of item (o, x): re-arm x's counter of parity o for order o + 2 (it is zero: it
+// fired for (o, x), and no dependency of (o + 2, x) completes before (o, x) did), then notify
+// the dependents (dataflow3.h: dependents()).
+__device__ __forceinline__ void df_complete(const TileGrid3& g, unsigned* cnt, unsigned* slots, unsigned qmask,
+                                            DataflowShared* sh, int o, int x) {
+    if (o + 2 < 8)
+        atomicAdd(cnt + (x >> 2), (unsigned)dep_count(g, o + 2, x) << (8u * (unsigned)(x & 3) + 4u * (unsigned)(o & 1)));
+    __threadfence_block();
+    if (o < 7) df_notify(cnt, slots, qmask, sh, x, o + 1);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int y = tile_neighbour(g, x, a, s);
+            if (y < 0) continue;
+            if (side_upstream(o, a, 1 - s)) df_notify(cnt, slots, qmask, sh, y, o);
+            if (o < 7 && !side_upstream(o + 1, a, 1 - s)) df_notify(cnt, slots, qmask, sh, y, o + 1);
+        }
+}
+
+// The warps' part of one outer iteration of instance inst.
 template <int KIND>
-__global__ void __launch_bounds__(kMaxPWarps * 32) sweep3d_persistent(const Sweep3Args A, const int nact,
-                                                                     const int maxiter, int* __restrict__ queue,
-                                                                     int* __restrict__ result) {
+__device__ __forceinline__ void df_iteration(const Sweep3Args& A, const int inst, const int iter, const TileGrid3& g,
+                                             unsigned* cnt, unsigned* slots, const unsigned qmask,
+                                             DataflowShared* sh, unsigned char* wsm, const int lane, const int nw) {
+    const int total = 8 * A.ntiles;
+    const int* dirty = A.dirty + (long long)inst * A.ntiles;
+    int last_done = -1;
+    unsigned long long idle_since = 0;
+    for (;;) {
+        if (*(volatile int*)&sh->abort) return;   // a stalled block gives up (warp-uniform read)
+        // ---- take up to 32 ready items, about this warp's share of the ring
+        unsigned h = 0;
+        int n = 0;
+        if (lane == 0) {
+            for (int tries = 0; tries < 32; ++tries) {
+                const unsigned hh = *(volatile unsigned*)&sh->head, tt = *(volatile unsigned*)&sh->tail;
+                const int avail = (int)(tt - hh);
+                if (avail <= 0) break;
+                const int want = min(32, max(1, avail / nw));
+                if (atomicCAS(&sh->head, hh, hh + (unsigned)want) == hh) { h = hh; n = want; break; }
+            }
+        }
+        n = __shfl_sync(0xffffffffu, n, 0);
+        h = __shfl_sync(0xffffffffu, h, 0);
+        if (n == 0) {
+            const int d = *(volatile int*)&sh->done;
+            if (d >= total || *(volatile int*)&sh->abort) return;
+            if (lane == 0) {   // nothing ready while other warps work: wait, bounded
+                const unsigned long long now = global_ns();
+                if (d != last_done) { last_done = d; idle_since = now; }
+                else if (now - idle_since > 2000000000ull) *(volatile int*)&sh->abort = 1;
+            }
+            __nanosleep(128);
+            __syncwarp();
+            continue;
+        }
+        unsigned e = kSlotEmpty;
+        if (lane < n) {
+            unsigned* slot = slots + ((h + (unsigned)lane) & qmask);
+            // the item's producer reserved this position before we took it: it is being written
+            for (int spin = 0; (e = atomicExch(slot, kSlotEmpty)) == kSlotEmpty; ++spin)
+                if (spin > (1 << 22) || *(volatile int*)&sh->abort) { *(volatile int*)&sh->abort = 1; break; }
+        }
+        __threadfence_block();
+        const bool have = e != kSlotEmpty;
+        const int x = (int)(e >> 3), o = (int)(e & 7u);
+        int dm = 0;
+        bool due = false;
+        if (have) {
+            dm = __ldcg(dirty + x);
+            due = tile_due<KIND>(dm, o);
+        }
+        const unsigned dmask = __ballot_sync(0xffffffffu, due);
+        const int mine = dmask ? __ffs(dmask) - 1 : -1;
+        int ncomp = 0;
+        if (have && !due) {   // locked in this order: nothing to compute
+            df_complete(g, cnt, slots, qmask, sh, o, x);
+            ncomp = 1;
+        }
+        if (due && lane != mine) df_push(slots, qmask, sh, e);   // for an idle warp
+        if (mine >= 0) {
+            const int ex = __shfl_sync(0xffffffffu, x, mine), eo = __shfl_sync(0xffffffffu, o, mine);
+            const int edm = __shfl_sync(0xffffffffu, dm, mine);
+            const int tj = ex % g.nbj, ti = (ex / g.nbj) % g.nbi, tk = ex / (g.nbj * g.nbi);
+            process_tile<KIND, true>(A, inst, ex, tk, ti, tj, eo, iter, edm, wsm, lane);
+            __threadfence_block();   // the tile's field and lock words before its dependents start
+            __syncwarp();
+            if (lane == 0) {
+                df_complete(g, cnt, slots, qmask, sh, eo, ex);
+                ++ncomp;
+            }
+        }
+        const int c = __reduce_add_sync(0xffffffffu, ncomp);
+        if (lane == 0 && c) atomicAdd(&sh->done, c);
+    }
+}
+
+// Warps per block of the dataflow kernel, at most: what 227 KB of shared memory holds beside
+// the counters and ring of an 8192-tile grid (one FP32 box per warp for the FP32 forward, 17.3 KB
+// otherwise), so that the register budget of a thread follows the block size.
+template <int KIND>
+__host__ __device__ constexpr int df_max_warps() {
+    return warp_smem_bytes<KIND>() <= 9000 ? 22 : 11;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(df_max_warps<KIND>() * 32, 1) sweep3d_dataflow(const Sweep3Args A, const int nact,
+                                                                      const int maxiter, int* __restrict__ queue,
+                                                                      int* __restrict__ result, const int qcap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_item, s_cnt;
-    __shared__ int s_list[kMaxPWarps * 32];
-    __shared__ int s_dm[kMaxPWarps * 32];
+    __shared__ DataflowShared sh;
+    constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
     const int nthr = blockDim.x, nw = nthr >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* wsm = smem_raw + warp * warp_smem_bytes<KIND>();
+    const int ntiles = A.ntiles, ncw = (ntiles + 3) >> 2;
+    unsigned* cnt = reinterpret_cast<unsigned*>(smem_raw + nw * warp_smem_bytes<KIND>());
+    unsigned* slots = cnt + ncw;
+    const unsigned qmask = (unsigned)qcap - 1u;
+    const TileGrid3 g{A.nbk, A.nbi, A.nbj};
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        if (threadIdx.x == 0) sh.item = atomicAdd(queue, 1);
         __syncthreads();
-        const int item = s_item;
+        const int item = sh.item;
         __syncthreads();
         if (item >= nact) return;   // block-uniform
         const int inst = A.act[item];
-        int* diff = A.diff + (long long)inst * A.ntiles;
-        const int* dirty = A.dirty + (long long)inst * A.ntiles;
+        int* diff = A.diff + (long long)inst * ntiles;
+        const int* dirty = A.dirty + (long long)inst * ntiles;
         int it = 0;
-        bool moved = true;
+        bool moved = true, aborted = false;
         while (it < maxiter) {
-            for (int t = threadIdx.x; t < A.ntiles; t += nthr) diff[t] = 0;
-            __syncthreads();
-            for (int dir = 0; dir < 8; ++dir) {
-                for (int d = 0; d < A.ndiag; ++d) {
-                    const int d0 = A.diag_off[d], cnt = A.diag_off[d + 1] - d0;
-                    for (int c0 = 0; c0 < cnt; c0 += nthr) {
-                        if (threadIdx.x == 0) s_cnt = 0;
-                        __syncthreads();
-                        const int idx = c0 + threadIdx.x;
-                        if (idx < cnt) {
-                            int tk, ti, tj;
-                            const int tid = tile_of(A, A.diag_tiles[d0 + idx], dir, tk, ti, tj);
-                            const int dm = __ldcg(dirty + tid);
-                            if (tile_due<KIND>(dm, dir)) {
-                                const int slot = atomicAdd(&s_cnt, 1);
-                                s_list[slot] = idx;
-                                s_dm[slot] = dm;
-                            }
-                        }
-                        __syncthreads();
-                        const int n = s_cnt;
-                        for (int q = warp; q < n; q += nw) {
-                            int tk, ti, tj;
-                            const int tid = tile_of(A, A.diag_tiles[d0 + s_list[q]], dir, tk, ti, tj);
-                            process_tile<KIND, true>(A, inst, tid, tk, ti, tj, dir, it, s_dm[q], wsm, lane);
-                        }
-                        __syncthreads();
-                    }
+            // counters of orders 0 and 1, an empty ring, cleared per-tile change flags
+            for (int w = threadIdx.x; w < ncw; w += nthr) {
+                unsigned v = 0;
+                for (int b = 0; b < 4; ++b) {
+                    const int x = 4 * w + b;
+                    if (x < ntiles) v |= (unsigned)(dep_count(g, 0, x) | (dep_count(g, 1, x) << 4)) << (8 * b);
                 }
+                cnt[w] = v;
             }
-            int any = 0;
-            for (int t = threadIdx.x; t < A.ntiles; t += nthr) any |= __ldcg(diff + t);
+            for (int q = threadIdx.x; q < qcap; q += nthr) slots[q] = kSlotEmpty;
+            for (int t = threadIdx.x; t < ntiles; t += nthr) diff[t] = 0;
+            if (threadIdx.x == 0) {
+                sh.head = 0;
+                sh.tail = 1;
+                sh.done = 0;
+                sh.abort = 0;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) slots[0] = (unsigned)first_tile(g) << 3;   // (order 0, first tile)
+            __syncthreads();
+            df_iteration<KIND>(A, inst, it, g, cnt, slots, qmask, &sh, wsm, lane, nw);
+            __syncthreads();
+            if (sh.abort) { aborted = true; break; }   // block-uniform
+            // convergence: some tile moved in this iteration / some tile still due in some order
+            int any = 0, due = 0;
+            for (int t = threadIdx.x; t < ntiles; t += nthr) {
+                any |= __ldcg(diff + t);
+                const int dm = __ldcg(dirty + t);
+                due |= (kSelective ? (dm & (dm >> 8)) : dm) & 0xff;
+            }
             any = __syncthreads_or(any);
+            due = __syncthreads_or(due);
             ++it;
-            if (!any) {
-                moved = false;
-                break;
-            }
+            if (!any) { moved = false; break; }
+            // moved, but every tile is a fixed point of its update: the next iteration would
+            // change nothing and pass the test; it is counted without running
+            if (!due && it < maxiter) { ++it; moved = false; break; }
         }
-        if (threadIdx.x == 0) result[inst] = it | (moved ? (1 << 30) : 0);
+        if (threadIdx.x == 0) result[inst] = it | (moved ? (1 << 30) : 0) | (aborted ? (1 << 29) : 0);
+        if (aborted) {
+            if (threadIdx.x == 0) atomicOr(queue + 1, 1);   // the host reports the stall
+            return;                                        // block-uniform
+        }
     }
 }
 
@@ -1023,26 +1184,27 @@ static pfast_status launch_one(const Sweep3Args& a, int d0, int tiles, int nact,
     return PFAST_OK;
 }
 
-template <int KIND>
-static pfast_status persistent_attr(int warps) {
-    static int set_for = 0;
-    const int smem = warps * warp_smem_bytes<KIND>();
-    if (set_for < smem) {
-        PFAST_CUDA_TRY(cudaFuncSetAttribute(sweep3d_persistent<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        set_for = smem;
-    }
-    return PFAST_OK;
+// Dataflow schedule: shared memory of a block = its warps' tile boxes + the dependency
+// counters (one byte per tile) + the ring of ready items (a power of two >= ntiles words).
+static int dataflow_qcap(int ntiles) {
+    int q = 1;
+    while (q < ntiles) q <<= 1;
+    return q;
+}
+
+static size_t dataflow_extra_bytes(int ntiles) {
+    return (size_t)4 * ((ntiles + 3) / 4) + (size_t)4 * dataflow_qcap(ntiles);
 }
 
 template <int KIND>
-static pfast_status persistent_shape_k(int nact, int* warps, int* blocks) {
-    static std::map<std::pair<int, int>, std::pair<int, int>> cache;   // (device, nact) -> (warps, blocks)
+static pfast_status dataflow_shape_k(int ntiles, int nact, int* warps, int* blocks) {
+    static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;   // (device, ntiles, nact)
     static std::mutex mu;
     int dev = 0, sms = 0, smem_max = 0;
     PFAST_CUDA_TRY(cudaGetDevice(&dev));
     {
-        std::lock_guard<std::mutex> g(mu);
-        auto it = cache.find({dev, nact});
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(std::make_tuple(dev, ntiles, nact));
         if (it != cache.end()) {
             *warps = it->second.first;
             *blocks = it->second.second;
@@ -1051,65 +1213,61 @@ static pfast_status persistent_shape_k(int nact, int* warps, int* blocks) {
     }
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const int need = std::max(1, (nact + sms - 1) / sms);   // blocks each SM must hold at once
-    const int w_cap = std::max(1, std::min(kMaxPWarps, (smem_max - 8192) / warp_smem_bytes<KIND>()));
-    int best_w = 1, best_b = 1;
-    for (int w = w_cap; w >= 1; --w) {
-        PFAST_TRY(persistent_attr<KIND>(w));
-        int per_sm = 0;
-        PFAST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep3d_persistent<KIND>, w * 32,
-                                                                     (size_t)w * warp_smem_bytes<KIND>()));
-        if (per_sm >= need || w == 1) {
-            best_w = w;
-            best_b = std::max(1, per_sm);
-            break;
-        }
+    const long long room = (long long)smem_max - 256 - (long long)dataflow_extra_bytes(ntiles);
+    const int w = (int)std::min<long long>(df_max_warps<KIND>(), room / warp_smem_bytes<KIND>());
+    if (ntiles > kDataflowMaxTiles || w < 1) {
+        *warps = 0;
+        *blocks = 0;
+        return PFAST_OK;
     }
-    *warps = best_w;
-    *blocks = std::min(nact, best_b * sms);
-    std::lock_guard<std::mutex> g(mu);
-    cache[{dev, nact}] = {*warps, *blocks};
+    const size_t smem = (size_t)w * warp_smem_bytes<KIND>() + dataflow_extra_bytes(ntiles);
+    PFAST_CUDA_TRY(cudaFuncSetAttribute(sweep3d_dataflow<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    PFAST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep3d_dataflow<KIND>, w * 32, smem));
+    *warps = w;
+    *blocks = std::max(1, std::min(nact, std::max(1, per_sm) * sms));
+    std::lock_guard<std::mutex> lk(mu);
+    cache[std::make_tuple(dev, ntiles, nact)] = {*warps, *blocks};
     return PFAST_OK;
 }
 
 template <int KIND>
-static pfast_status launch_persistent_k(const Sweep3Args& a, int nact, int maxiter, int* queue, int* result, int warps,
-                                        int blocks, cudaStream_t st) {
-    PFAST_TRY(persistent_attr<KIND>(warps));
-    sweep3d_persistent<KIND><<<blocks, warps * 32, (size_t)warps * warp_smem_bytes<KIND>(), st>>>(a, nact, maxiter,
-                                                                                                  queue, result);
+static pfast_status launch_dataflow_k(const Sweep3Args& a, int nact, int maxiter, int* queue, int* result, int warps,
+                                      int blocks, cudaStream_t st) {
+    const size_t smem = (size_t)warps * warp_smem_bytes<KIND>() + dataflow_extra_bytes(a.ntiles);
+    sweep3d_dataflow<KIND><<<blocks, warps * 32, smem, st>>>(a, nact, maxiter, queue, result, dataflow_qcap(a.ntiles));
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "persistent sweep launch", __FILE__, __LINE__);
+    if (e != cudaSuccess) return cuda_fail(e, "dataflow sweep launch", __FILE__, __LINE__);
     return PFAST_OK;
 }
 
-pfast_status persistent_shape(int kind, int nact, int* warps, int* blocks) {
+pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks) {
     switch (kind) {
-        case kFwdPlain64: return persistent_shape_k<kFwdPlain64>(nact, warps, blocks);
-        case kFwdFast32: return persistent_shape_k<kFwdFast32>(nact, warps, blocks);
-        case kFwdPolish64: return persistent_shape_k<kFwdPolish64>(nact, warps, blocks);
-        case kAdjPlain64: return persistent_shape_k<kAdjPlain64>(nact, warps, blocks);
-        case kAdjFast32: return persistent_shape_k<kAdjFast32>(nact, warps, blocks);
-        case kAdjPolish64: return persistent_shape_k<kAdjPolish64>(nact, warps, blocks);
+        case kFwdPlain64: return dataflow_shape_k<kFwdPlain64>(ntiles, nact, warps, blocks);
+        case kFwdFast32: return dataflow_shape_k<kFwdFast32>(ntiles, nact, warps, blocks);
+        case kFwdPolish64: return dataflow_shape_k<kFwdPolish64>(ntiles, nact, warps, blocks);
+        case kAdjPlain64: return dataflow_shape_k<kAdjPlain64>(ntiles, nact, warps, blocks);
+        case kAdjFast32: return dataflow_shape_k<kAdjFast32>(ntiles, nact, warps, blocks);
+        case kAdjPolish64: return dataflow_shape_k<kAdjPolish64>(ntiles, nact, warps, blocks);
     }
     set_last_error("unknown sweep kind %d", kind);
     return PFAST_ERR_INVALID;
 }
 
-pfast_status launch_sweep3_persistent(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
-                                      int warps, int blocks, cudaStream_t st) {
+pfast_status launch_sweep3_dataflow(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
+                                    int warps, int blocks, cudaStream_t st) {
     if (nact <= 0 || maxiter <= 0) return PFAST_OK;
-    if (warps < 1 || warps > kMaxPWarps || blocks < 1) {
-        set_last_error("persistent sweep: bad shape (%d warps, %d blocks)", warps, blocks);
+    if (warps < 1 || warps > 32 || blocks < 1 || a.ntiles > kDataflowMaxTiles) {
+        set_last_error("dataflow sweep: bad shape (%d warps, %d blocks, %d tiles)", warps, blocks, a.ntiles);
         return PFAST_ERR_INVALID;
     }
     switch (kind) {
-        case kFwdPlain64: return launch_persistent_k<kFwdPlain64>(a, nact, maxiter, queue, result, warps, blocks, st);
-        case kFwdFast32: return launch_persistent_k<kFwdFast32>(a, nact, maxiter, queue, result, warps, blocks, st);
-        case kFwdPolish64: return launch_persistent_k<kFwdPolish64>(a, nact, maxiter, queue, result, warps, blocks, st);
-        case kAdjPlain64: return launch_persistent_k<kAdjPlain64>(a, nact, maxiter, queue, result, warps, blocks, st);
-        case kAdjFast32: return launch_persistent_k<kAdjFast32>(a, nact, maxiter, queue, result, warps, blocks, st);
-        case kAdjPolish64: return launch_persistent_k<kAdjPolish64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kFwdPlain64: return launch_dataflow_k<kFwdPlain64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kFwdFast32: return launch_dataflow_k<kFwdFast32>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kFwdPolish64: return launch_dataflow_k<kFwdPolish64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kAdjPlain64: return launch_dataflow_k<kAdjPlain64>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kAdjFast32: return launch_dataflow_k<kAdjFast32>(a, nact, maxiter, queue, result, warps, blocks, st);
+        case kAdjPolish64: return launch_dataflow_k<kAdjPolish64>(a, nact, maxiter, queue, result, warps, blocks, st);
     }
     set_last_error("unknown sweep kind %d", kind);
     return PFAST_ERR_INVALID;

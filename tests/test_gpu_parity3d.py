@@ -246,6 +246,41 @@ def test_persistent_schedule_matches_per_diagonal(ctx):
     sv.close()
 
 
+@pytest.mark.parametrize("shape,h", [((22, 40, 100), (20.0, 20.0, 20.0)), ((13, 17, 70), (10.0, 12.5, 8.0))])
+def test_dataflow_schedule_matches_per_diagonal_on_many_tiles(ctx, shape, h):
+    """A grid of 6 x 5 x 4 (and 4 x 3 x 3) tiles with a few sources: in the dataflow schedule
+    one block solves a source with its sweep orders overlapping as the tile dependencies allow.
+    Plain and mixed fields, gradients, misfits and iteration counts are bit-identical to the
+    per-diagonal launches, and plain equals the oracle."""
+    import torch
+    from oracle import port
+    pg = _pg()
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 31)
+    nz, nr, nc = shape
+    sv = pg.Survey3D(ctx, nr, nc, nz, *h, src, srnum, rec, nxyz, tobs)
+    d_vp = torch.from_numpy(vp).cuda()
+    out = {}
+    for prec in (pg.PFAST_PLAIN_FP64, pg.PFAST_MIXED):
+        for sched in (pg._capi.PFAST_SCHEDULE_DIAGONAL, pg._capi.PFAST_SCHEDULE_PERSISTENT):
+            g, e, st = sv.eval(d_vp, precision=prec, schedule=sched)
+            pk, _ = sv.forward(d_vp, precision=prec, schedule=sched)
+            out[prec, sched] = (g.cpu().numpy(), e, pk.cpu().numpy(), st)
+        a, b = out[prec, 1], out[prec, 2]
+        assert bits_equal(a[0], b[0]) and a[1] == b[1] and bits_equal(a[2], b[2])
+        for k in ("fwd_iters_max", "adj_iters_max", "fwd32_iters_max", "adj32_iters_max", "fwd_node_updates",
+                  "adj_node_updates", "not_converged"):
+            assert a[3][k] == b[3][k], k
+        assert b[3]["launches"] < a[3]["launches"]
+    g0, e0, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h, nthreads=8)
+    assert bits_equal(out[pg.PFAST_PLAIN_FP64, 2][0], g0) and out[pg.PFAST_PLAIN_FP64, 2][1] == e0
+    # an iteration cap: both schedules stop after the same two iterations with the same fields
+    g1, e1, s1 = sv.eval(d_vp, precision=pg.PFAST_PLAIN_FP64, maxswp=2, schedule=1)
+    g2, e2, s2 = sv.eval(d_vp, precision=pg.PFAST_PLAIN_FP64, maxswp=2, schedule=2)
+    assert bits_equal(g1.cpu().numpy(), g2.cpu().numpy()) and e1 == e2
+    assert s1["not_converged"] == s2["not_converged"] and s1["fwd_iters_max"] == s2["fwd_iters_max"] <= 2
+    sv.close()
+
+
 def test_near_source_initialisation_reduces_the_source_error(ctx):
     """Opt-in near-source start (not in the reference): in a homogeneous medium, where the exact
     traveltime is distance / v, starting the nodes within 4 nodes of the source from the
