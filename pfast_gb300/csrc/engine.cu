@@ -10,6 +10,7 @@
 // tolerance.  Converged sources retire from the batch; the others keep sweeping.
 
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -241,9 +242,19 @@ static pfast_status iteration_graph(pfast_ctx* ctx, const Sweep3Args& a, int kin
     return PFAST_OK;
 }
 
+// Whether the tiles of a phase can move in 16-byte vectors: every grid row of the field (and of
+// the FP32 adjoint's staged traveltime) starts on a 16-byte boundary.
+static int rows_aligned(const Sweep3Args& a, int kind) {
+    const int esz = (kind == kFwdFast32 || kind == kAdjFast32) ? 4 : 8;
+    if (a.nc % (16 / esz) != 0 || reinterpret_cast<uintptr_t>(a.field) % 16 != 0) return 0;
+    if (kind == kAdjFast32 && reinterpret_cast<uintptr_t>(a.aux) % 16 != 0) return 0;
+    return 1;
+}
+
 pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable3& dt, int nb,
                          std::vector<int>& active, int maxiter, int* iters, long long nodes_per_sweep,
                          long long* node_updates, int* not_conv, double* ms_acc) {
+    a.vec_rows = rows_aligned(a, kind);
     PFAST_TRY(ctx->act.ensure(sizeof(int) * nb));
     PFAST_TRY(ctx->changed.ensure(sizeof(int) * nb));
     PFAST_TRY(ctx->h_act.ensure(sizeof(int) * nb));

@@ -41,6 +41,9 @@ struct Sweep3Args {
     float polish_floor;       // polish sweeps: corrections at or below this are dropped (seconds;
                               // adjoint: relative to 1 + |lambda|)
     unsigned long long* work; // per instance: nodes of the tiles processed (executed node updates); may be null
+    int vec_rows;             // rows of the field (and of the FP32 adjoint's traveltime) start on 16-byte
+                              // boundaries: nc a multiple of 16 / element size, 16-byte aligned fields;
+                              // tiles then move in 16-byte vectors
     const int* dyn;           // per-diagonal launches of a replayed iteration graph: dyn[0] = outer
                               // iteration (instead of iter), dyn[1] = active instances (blocks with
                               // blockIdx.y >= dyn[1] exit); null: iter and the grid

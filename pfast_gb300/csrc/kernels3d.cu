@@ -285,22 +285,33 @@ __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm,
 }
 
 // ----------------------------------------------------------- tile I/O
-// Load the (TK+2)x(TI+2)x(TJ+2) halo box at origin (k0-1, i0-1, j0-1) into `box`
-// (plane stride PS, row stride HJ), one box row per warp instruction (lanes along
-// the row, coalesced); out-of-grid entries get `fill`.  Twelve rows are loaded
-// before they are stored, to keep many loads in flight.
-// COHERENT: the field, which the persistent kernel itself writes (other warps of the block
+// A tile's halo box is kept in shared memory in the coordinates of the current sweep order:
+// each axis is reversed where the sweep descends, so that every order walks the box the same
+// way.  Node (kf, if, jf) of the flipped tile lies at (kf+1)*PS + (if+1)*HJ + jf+1 and its
+// flipped upstream neighbours at -PS, -HJ, -1; a wavefront step of lanes (kf, if) touches
+// kf*(PS-1) + if*(HJ-1) + t, and with PS-1 = 8, HJ-1 = 1 (mod 32) the 32 lanes hit 32
+// distinct banks in every order (in grid coordinates the descending orders meet 2-way
+// conflicts).  Halo position z = 0..ek+1 around a tile of ek planes (grid plane k0-1+z) lies
+// at flipped zf = z where the sweep ascends along z, else ek+1-z; likewise rows and columns.
+//
+// load_box: the halo box at origin (k0-1, i0-1, j0-1), one box row per warp instruction
+// (lanes along the row, coalesced); out-of-grid entries get `fill`; the rows and columns
+// beyond a partial tile's halo are neither loaded nor stored (never read).  Twelve rows are
+// loaded before they are stored, to keep many loads in flight.
+// COHERENT: the field, which the dataflow kernel itself writes (other warps of the block
 // stored the neighbouring tiles): read through L2, not the read-only path.
 template <typename T, bool COHERENT>
-__device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0, int i0, int j0, int nz, int nr,
-                                         int nc, T fill, int lane) {
+__device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0, int i0, int j0, int ek, int ei,
+                                         int ej, bool pz, bool py, bool px, int nz, int nr, int nc, T fill, int lane) {
     constexpr int NROW = HK * HI;
     constexpr int RB = 12;
     static_assert(NROW % RB == 0 && HJ - 32 <= 32, "row batching");
     const long long plane = (long long)nr * nc;
     const int gj0 = j0 - 1 + lane, gj1 = j0 + 31 + lane;
-    const bool c0 = (unsigned)gj0 < (unsigned)nc;
-    const bool c1 = lane < HJ - 32 && (unsigned)gj1 < (unsigned)nc;
+    const bool s0 = lane <= ej + 1, s1 = lane < HJ - 32 && lane + 32 <= ej + 1;   // within the halo
+    const bool c0 = s0 && (unsigned)gj0 < (unsigned)nc;
+    const bool c1 = s1 && (unsigned)gj1 < (unsigned)nc;
+    const int xf0 = px ? lane : ej + 1 - lane, xf1 = px ? lane + 32 : ej - 31 - lane;
 #pragma unroll 1
     for (int rb = 0; rb < NROW; rb += RB) {
         T v0[RB], v1[RB];
@@ -308,7 +319,7 @@ __device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0
         for (int u = 0; u < RB; ++u) {
             const int r = rb + u, z = r / HI, y = r - z * HI;
             const int gk = k0 - 1 + z, gi = i0 - 1 + y;
-            const bool rok = (unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr;
+            const bool rok = z <= ek + 1 && y <= ei + 1 && (unsigned)gk < (unsigned)nz && (unsigned)gi < (unsigned)nr;
             const T* row = g + gk * plane + (long long)gi * nc;
             if constexpr (COHERENT) {
                 v0[u] = (rok && c0) ? __ldcg(row + gj0) : fill;
@@ -321,11 +332,118 @@ __device__ __forceinline__ void load_box(T* box, const T* __restrict__ g, int k0
 #pragma unroll
         for (int u = 0; u < RB; ++u) {
             const int r = rb + u, z = r / HI, y = r - z * HI;
-            T* brow = box + z * PS + y * HJ;
-            brow[lane] = v0[u];
-            if (lane < HJ - 32) brow[32 + lane] = v1[u];
+            if (z > ek + 1 || y > ei + 1) continue;
+            T* brow = box + (pz ? z : ek + 1 - z) * PS + (py ? y : ei + 1 - y) * HJ;
+            if (s0) brow[xf0] = v0[u];
+            if (s1) brow[xf1] = v1[u];
         }
     }
+}
+
+// Vector form of load_box, for grids whose rows start on 16-byte boundaries (ncols a multiple of
+// V = 16 / sizeof(T) and a 16-byte aligned field): box rows are read as aligned V-element vectors
+// from grid column j0 - V on, so the halo columns j0 - 1 and j0 + ej come with their vectors
+// (a vector lies wholly inside or outside the grid).  The first MV = TJ / V vectors of each row
+// (columns j0 - V .. j0 + TJ - V - 1) are read by 32 / MV rows of lanes at a time; the last two
+// (columns j0 + TJ - V .. j0 + TJ + V - 1) by 16 rows of lane pairs.  A lane's columns, and so its
+// flipped box positions, are fixed for the whole load.
+template <typename T, bool COHERENT>
+__device__ __forceinline__ void load_box_vec(T* box, const T* __restrict__ g, int k0, int i0, int j0, int ek, int ei,
+                                             int ej, bool pz, bool py, bool px, int nz, int nr, int nc, T fill,
+                                             int lane) {
+    using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int V = 16 / sizeof(T);
+    constexpr int MV = TJ / V;          // main vectors per row: 8 (FP32) or 16 (FP64)
+    constexpr int RPI = 32 / MV;        // rows per main pass: 4 or 2
+    constexpr int NROW = HK * HI;
+    const long long plane = (long long)nr * nc;
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+        const int q = part == 0 ? lane % MV : MV + (lane & 1);   // the lane's vector in the row
+        const int rsub = part == 0 ? lane / MV : lane >> 1;      // its row within a pass
+        const int rstep = part == 0 ? RPI : 16;
+        const int gx = j0 - V + q * V;                           // grid column of the vector's first element
+        const bool vin = gx >= 0 && gx < nc;
+        int xf[V];
+        bool xs[V];
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+            const int bx = gx + e - (j0 - 1);                    // halo-box column
+            xs[e] = bx >= 0 && bx <= ej + 1;
+            xf[e] = px ? bx : ej + 1 - bx;
+        }
+        constexpr int BATCH = 8;
+#pragma unroll 1
+        for (int r0 = 0; r0 < NROW; r0 += BATCH * rstep) {
+            VT v[BATCH];
+#pragma unroll
+            for (int u = 0; u < BATCH; ++u) {
+                const int r = r0 + u * rstep + rsub, z = r / HI, y = r - z * HI;
+                const int gk = k0 - 1 + z, gi = i0 - 1 + y;
+                const bool ok = vin && r < NROW && z <= ek + 1 && y <= ei + 1 && (unsigned)gk < (unsigned)nz &&
+                                (unsigned)gi < (unsigned)nr;
+                const VT* src = reinterpret_cast<const VT*>(g + gk * plane + (long long)gi * nc + gx);
+                if (ok) v[u] = COHERENT ? __ldcg(src) : __ldg(src);
+                else {
+                    T* f = reinterpret_cast<T*>(&v[u]);
+#pragma unroll
+                    for (int e = 0; e < V; ++e) f[e] = fill;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < BATCH; ++u) {
+                const int r = r0 + u * rstep + rsub, z = r / HI, y = r - z * HI;
+                if (r >= NROW || z > ek + 1 || y > ei + 1) continue;
+                T* brow = box + (pz ? z : ek + 1 - z) * PS + (py ? y : ei + 1 - y) * HJ;
+                const T* f = reinterpret_cast<const T*>(&v[u]);
+#pragma unroll
+                for (int e = 0; e < V; ++e)
+                    if (xs[e]) brow[xf[e]] = f[e];
+            }
+        }
+    }
+}
+
+// Vector write-back of the tile's interior (same alignment condition; ej is then a multiple of
+// V): lane (row of a pass, vector) gathers V flipped box entries and stores them at once.
+template <typename T>
+__device__ __forceinline__ void store_tile_vec(T* __restrict__ fld, const T* box, int k0, int i0, int j0, int ek,
+                                               int ei, int ej, bool pz, bool py, bool px, int nr, int nc, int lane) {
+    using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int V = 16 / sizeof(T);
+    constexpr int MV = TJ / V, RPI = 32 / MV;
+    const long long plane = (long long)nr * nc;
+    const int q = lane % MV, rsub = lane / MV;
+    const bool qok = q * V < ej;
+#pragma unroll 4
+    for (int r0 = 0; r0 < TK * TI; r0 += RPI) {
+        const int r = r0 + rsub, rk = r / TI, ri = r - rk * TI;
+        if (!qok || rk >= ek || ri >= ei) continue;
+        const int base = ((pz ? rk : ek - 1 - rk) + 1) * PS + ((py ? ri : ei - 1 - ri) + 1) * HJ + 1;
+        VT v;
+        T* f = reinterpret_cast<T*>(&v);
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+            const int rj = q * V + e;
+            f[e] = box[base + (px ? rj : ej - 1 - rj)];
+        }
+        *reinterpret_cast<VT*>(fld + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + q * V) = v;
+    }
+}
+
+// Index of tile node (rk, ri, rj) (tile coordinates, grid orientation) in the flipped box.
+__device__ __forceinline__ int box_index(int rk, int ri, int rj, int ek, int ei, int ej, bool pz, bool py, bool px) {
+    return ((pz ? rk : ek - 1 - rk) + 1) * PS + ((py ? ri : ei - 1 - ri) + 1) * HJ + (px ? rj : ej - 1 - rj) + 1;
+}
+
+// r[o] = m[o ^ c] for the 8 order bits of m: an order mask of the flipped coordinates of sweep
+// order dir, mapped to grid orders with c = ~dir & 7 (order o in grid terms ascends along an
+// axis in flipped terms exactly where o and dir agree).
+__device__ __forceinline__ unsigned xor_permute8(unsigned m, int c) {
+    if (c & 1) m = ((m & 0x55u) << 1) | ((m & 0xaau) >> 1);
+    if (c & 2) m = ((m & 0x33u) << 2) | ((m & 0xccu) >> 2);
+    if (c & 4) m = ((m & 0x0fu) << 4) | ((m & 0xf0u) >> 4);
+    return m;
 }
 
 // ----------------------------------------------------------- octant selection (polish)
@@ -405,7 +523,9 @@ __device__ __forceinline__ bool tile_due(int dm, int dir) {
 // One warp processes one tile (inst, tid) in sweep order dir, outer iteration iter; dmask is
 // the tile's lock word as read by the caller, which has checked tile_due.  wsm: the warp's
 // shared-memory slice.  COHERENT: the field may have been written by this same kernel launch
-// (persistent schedule), so it is read through L2 instead of the read-only path.
+// (dataflow schedule), so it is read through L2 instead of the read-only path.
+// The box is in the flipped coordinates of order dir (see load_box); the lanes (kf, if) walk
+// their pencils jf = 0..ej-1 so that step t updates the flipped hyperplane kf+if+jf = t.
 template <int KIND, bool COHERENT>
 __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst, const int tid, const int tk,
                                              const int ti, const int tj, const int dir, const int iter,
@@ -424,8 +544,9 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     // instruction).  The plain kinds compare with a snapshot taken at the tile's first
     // processing in the iteration, as the reference's isconv does.
     constexpr bool kSnap = KIND == kFwdPlain64 || KIND == kAdjPlain64;
-    // The tile's lock word as lane 0 last wrote it.  Face neighbours run in other launches and
-    // no other tile of this launch writes it, so it is composed here without reading it back.
+    // The tile's lock word as lane 0 last wrote it.  Face neighbours are never processed at the
+    // same time (per-diagonal: other launches; dataflow: the dependencies), so it is composed
+    // here without reading it back.
     int dword = kSelective ? (dmask & ~obit) : 0;
     if (lane == 0) {
         dirty[tid] = dword;
@@ -446,20 +567,25 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     // ---- stage the field halo box (out-of-grid: +inf for the forward so that the
     // neighbour minimum reduces to the one-sided rule at faces; never read by the adjoint)
     const Real fill = ADJ ? Real(0) : Real(INFINITY);
-    load_box<Real, COHERENT>(box, fld, k0, i0, j0, nz, nr, nc, fill, lane);
+    if (A.vec_rows) load_box_vec<Real, COHERENT>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
+    else load_box<Real, COHERENT>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
 
     // ---- auxiliary data
-    unsigned fixed_bits = 0;
+    unsigned fixed_bits = 0;   // adjoint: fixed nodes of this lane's pencil, bit jf (flipped position)
     const int lkf = lane / TI, lif = lane % TI;
     const bool lane_ok = lkf < ek && lif < ei;
-    const int lk = pz ? lkf : ek - 1 - lkf;
+    const int lk = pz ? lkf : ek - 1 - lkf;   // the lane's position in the tile, grid orientation
     const int li = py ? lif : ei - 1 - lif;
     if constexpr (ADJ) {
-        if constexpr (!TWIN)
-            load_box<Aux, false>(aux, reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride, k0, i0, j0, nz, nr, nc,
-                                 Aux(0), lane);
-        if (lane_ok)
-            fixed_bits = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
+        if constexpr (!TWIN) {
+            const Aux* tb = reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride;
+            if (A.vec_rows) load_box_vec<Aux, false>(aux, tb, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, Aux(0), lane);
+            else load_box<Aux, false>(aux, tb, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, Aux(0), lane);
+        }
+        if (lane_ok) {
+            const unsigned fb = A.mask[inst * A.mask_stride + ((long long)(k0 + lk) * nr + (i0 + li)) * A.wpr + (j0 >> 5)];
+            fixed_bits = px ? fb : (__brev(fb) >> (32 - ej));
+        }
     }
 
     // ---- snapshot at the tile's first processing in this outer iteration (its values are
@@ -473,7 +599,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                 const int rk = m / TI, ri = m % TI;
                 if (rk < ek && ri < ei && lane < ej)
                     snp[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
-                        box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+                        box[box_index(rk, ri, lane, ek, ei, ej, pz, py, px)];
             }
             if (lane == 0) stamp[tid] = iter;
         }
@@ -482,21 +608,32 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
     // ---- wavefront over the tile's node hyperplanes
     const int gk = k0 + lk, gi = i0 + li;
-    const int cbase = (lk + 1) * PS + (li + 1) * HJ + 1;
     const int steps = ek + ei + ej - 2;
-    int sk = -1, si = -1, sj = -1;
-    if constexpr (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
+    const int toff = lane_ok ? lkf + lif : (1 << 20);   // flipped column of step t: t - toff
+    const int cl = (lkf + 1) * PS + (lif + 1) * HJ + 1 - lkf - lif;   // box index of step t: cl + t
+    const int dj = px ? 1 : -1, gjA = j0 + (px ? 0 : ej - 1);      // grid column of jf: gjA + dj*jf
+    int sk = -1, si = -1, sj = -1, qkqi = 0;
+    bool near_src = false;   // forward: the tile meets the fixed region around the source
+    if constexpr (!ADJ) {
+        sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2];
+        const int ddk = max(0, max(k0 - sk, sk - (k0 + ek - 1))), ddi = max(0, max(i0 - si, si - (i0 + ei - 1)));
+        const int ddj = max(0, max(j0 - sj, sj - (j0 + ej - 1)));
+        near_src = ddk * ddk + ddi * ddi + ddj * ddj <= A.src_r2;
+        qkqi = (gk - sk) * (gk - sk) + (gi - si) * (gi - si);
+    }
     const bool row_interior = ADJ ? (gk >= 1 && gk <= nz - 2 && gi >= 1 && gi <= nr - 2) : true;
-    unsigned sel = 0;   // polish: orders in which some node of this lane's pencil is selected
+    unsigned sel = 0;   // polish: orders (flipped coordinates) in which some node of this lane's pencil is selected
     const long long rowbase = gk * plane + (long long)gi * nc;
-    bool chg = false, chg_jlo = false, chg_jhi = false;   // this lane's pencil changed (anywhere / at lj = 0 / at ej-1)
-    // Face marks: a changed face node that a node of the face neighbour depends on.  The
-    // plain kinds mark every changed face node (their tile skipping must stay exact).
-    // Elsewhere the dependency is one-directional: a forward update reads only neighbours
-    // below the node's value (the Godunov update and its Newton form exclude larger ones),
-    // and lambda at a node reads only neighbours of larger traveltime.
+    const Aux* srow = ADJ ? nullptr : reinterpret_cast<const Aux*>(A.aux) + rowbase;
+    bool chg = false;   // this lane's pencil changed
+    // Face marks in flipped terms (u: the upstream face of the sweep, d: the downstream one): a
+    // changed face node that a node of the face neighbour depends on.  The plain kinds mark
+    // every changed face node (their tile skipping must stay exact).  Elsewhere the dependency
+    // is one-directional: a forward update reads only neighbours below the node's value (the
+    // Godunov update and its Newton form exclude larger ones), and lambda at a node reads only
+    // neighbours of larger traveltime.
     constexpr bool kPrune = KIND != kFwdPlain64 && KIND != kAdjPlain64;
-    bool m_klo = false, m_khi = false, m_ilo = false, m_ihi = false;
+    bool m_zu = false, m_zd = false, m_yu = false, m_yd = false, m_xu = false, m_xd = false;
     bool restep = false;   // polish: some update left a remainder above the floor (visit again in this order)
     // FP32 bulk: some changed node feeds an in-tile node that this pass visited before it
     // (so the tile is not yet a fixed point of the update)
@@ -548,9 +685,9 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
 #pragma unroll 1
     for (int t = 0; t < steps; ++t) {
-        const int ljf = t - lkf - lif;
-        // adjoint: the traveltimes around this lane's node, in grid orientation
-        Aux Txm = Aux(0), Txp = Aux(0), Tym = Aux(0), Typ = Aux(0), Tzm = Aux(0), Tzp = Aux(0);
+        const int ljf = t - toff;
+        // adjoint: the traveltimes around this lane's node, flipped orientation (u: upstream)
+        Aux Tzu = Aux(0), Tzd = Aux(0), Tyu = Aux(0), Tyd = Aux(0), Txu = Aux(0), Txd = Aux(0);
         if constexpr (TWIN) {
             const Aux a = __shfl_sync(0xffffffffu, tm, (lane - TI) & 31);
             const Aux b = __shfl_sync(0xffffffffu, tp, (lane + TI) & 31);
@@ -560,37 +697,33 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             const Aux hkh = __shfl_sync(0xffffffffu, h0, 8 + lif);
             const Aux hil = __shfl_sync(0xffffffffu, h0, 16 + (lkf & 3));
             const Aux hih = __shfl_sync(0xffffffffu, h0, 20 + (lkf & 3));
-            const Aux zkm = lkf == 0 ? hkl : a, zkp = lkf == ek - 1 ? hkh : b;
-            const Aux yim = lif == 0 ? hil : c_, yip = lif == ei - 1 ? hih : d;
-            Tzm = pz ? zkm : zkp; Tzp = pz ? zkp : zkm;
-            Tym = py ? yim : yip; Typ = py ? yip : yim;
-            Txm = px ? tm : tp;   Txp = px ? tp : tm;
+            Tzu = lkf == 0 ? hkl : a; Tzd = lkf == ek - 1 ? hkh : b;
+            Tyu = lif == 0 ? hil : c_; Tyd = lif == ei - 1 ? hih : d;
+            Txu = tm; Txd = tp;
         }
-        if (lane_ok && ljf >= 0 && ljf < ej) {
-            const int lj = px ? ljf : ej - 1 - ljf;
-            const int c = cbase + lj;
-            const int gj = j0 + lj;
+        if ((unsigned)ljf < (unsigned)ej) {
+            const int c = cl + t;
+            const Real xu = box[c - 1], xd = box[c + 1], yu = box[c - HJ], yd = box[c + HJ];
+            const Real zu = box[c - PS], zd = box[c + PS];
             const Real old = box[c];
             Real nv = old;
             float dstep = INFINITY;   // polish: the size of this node's change
             if constexpr (ADJ && !TWIN) {   // FP32 bulk: the traveltimes from the staged box
-                t0 = aux[c]; Txm = aux[c - 1]; Txp = aux[c + 1]; Tym = aux[c - HJ]; Typ = aux[c + HJ];
-                Tzm = aux[c - PS]; Tzp = aux[c + PS];
+                t0 = aux[c]; Txu = aux[c - 1]; Txd = aux[c + 1]; Tyu = aux[c - HJ]; Tyd = aux[c + HJ];
+                Tzu = aux[c - PS]; Tzd = aux[c + PS];
             }
             if constexpr (!ADJ) {
-                const int qk = gk - sk, qi = gi - si, qj = gj - sj;
-                if (qk * qk + qi * qi + qj * qj > A.src_r2) {   // the source node (and the opt-in fixed region) stays
-                    const Aux s = __ldg(reinterpret_cast<const Aux*>(A.aux) + rowbase + gj);
+                const int gj = gjA + dj * ljf;
+                bool free_node = true;   // the source node (and the opt-in fixed region) stays
+                if (near_src) free_node = qkqi + (gj - sj) * (gj - sj) > A.src_r2;
+                if (free_node) {
+                    const Aux s = __ldg(srow + gj);
+                    // the neighbour minima are symmetric in the two neighbours of an axis
                     if constexpr (KIND == kFwdPlain64) {
-                        const double xa = min_nonneg(box[c + 1], box[c - 1]);
-                        const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
-                        const double zc = min_nonneg(box[c - PS], box[c + PS]);
-                        nv = min_nonneg(old, eik3_plain(xa, yb, zc, s, A.sp));
+                        nv = min_nonneg(old, eik3_plain(min_nonneg(xd, xu), min_nonneg(yd, yu), min_nonneg(zd, zu), s, A.sp));
                     } else if constexpr (KIND == kFwdFast32) {
                         // field values are >= +0 or +inf: fminf is the reference's MIN here
-                        const float xa = fminf(box[c + 1], box[c - 1]);
-                        const float yb = fminf(box[c - HJ], box[c + HJ]);
-                        const float zc = fminf(box[c - PS], box[c + PS]);
+                        const float xa = fminf(xd, xu), yb = fminf(yd, yu), zc = fminf(zd, zu);
                         nv = fminf(old, A.sp.iso ? eik3_fast_iso(xa, yb, zc, s * A.sp.df[0]) : eik3_fast(xa, yb, zc, s, A.sp));
                     } else {   // polish: one Newton step of the local Godunov equation (aux holds s^2, (s h)^2 when isotropic)
                         // Octant selection: if an axis is active (U0 above its smaller neighbour) and
@@ -598,43 +731,44 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                         // read a value the sweep has not refreshed; the node keeps its value and is
                         // updated by the sweep that visits its upwind neighbours first.  A Newton step
                         // is not monotone, so without this every sweep would move every node.
-                        // Integer compares of the bit patterns (values >= 0).
-                        const unsigned m = fwd_orders(dbits(old), dbits(box[c - 1]), dbits(box[c + 1]),
-                                                      dbits(box[c - HJ]), dbits(box[c + HJ]), dbits(box[c - PS]),
-                                                      dbits(box[c + PS]));
+                        // Integer compares of the bit patterns (values >= 0), in flipped terms: this
+                        // sweep is order 7 there (every axis ascending).
+                        const unsigned m = fwd_orders(dbits(old), dbits(xu), dbits(xd), dbits(yu), dbits(yd), dbits(zu),
+                                                      dbits(zd));
                         sel |= m;
-                        if (m & obit) {
-                            const double xa = min_nonneg(box[c + 1], box[c - 1]);
-                            const double yb = min_nonneg(box[c - HJ], box[c + HJ]);
-                            const double zc = min_nonneg(box[c - PS], box[c + PS]);
+                        if (m & 0x80u) {
                             bool big = false;
-                            nv = eik3_newton(old, xa, yb, zc, s, A.slow64, rowbase + gj, A.sp, A.polish_floor, big,
-                                             dstep);
+                            nv = eik3_newton(old, min_nonneg(xd, xu), min_nonneg(yd, yu), min_nonneg(zd, zu), s, A.slow64,
+                                             rowbase + gj, A.sp, A.polish_floor, big, dstep);
                             restep |= big;
                         }
                     }
                 }
             } else {
-                if (row_interior && gj >= 1 && gj <= nc - 2 && !((fixed_bits >> lj) & 1u)) {
+                const int gj = gjA + dj * ljf;
+                if (row_interior && gj >= 1 && gj <= nc - 2 && !((fixed_bits >> ljf) & 1u)) {
                     if constexpr (KIND == kAdjPlain64) {
-                        nv = adj3_plain(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
-                                        box[c - HJ], box[c + PS], box[c - PS], A.sp);
+                        // the reference's operand order, in grid orientation (m: index - 1, p: index + 1)
+                        const Real Lxp = px ? xd : xu, Lxm = px ? xu : xd, Lyp = py ? yd : yu, Lym = py ? yu : yd;
+                        const Real Lzp = pz ? zd : zu, Lzm = pz ? zu : zd;
+                        const Aux Txp = px ? Txd : Txu, Txm = px ? Txu : Txd, Typ = py ? Tyd : Tyu, Tym = py ? Tyu : Tyd;
+                        const Aux Tzp = pz ? Tzd : Tzu, Tzm = pz ? Tzu : Tzd;
+                        nv = adj3_plain(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, A.sp);
                     } else if constexpr (KIND == kAdjFast32) {
-                        nv = adj3_bulk(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
-                                       box[c - HJ], box[c + PS], box[c - PS], old, A.sp);
+                        // each axis's two neighbours enter alike: flipped orientation (d for p, u for m)
+                        nv = adj3_bulk(t0, Txd, Txu, Tyd, Tyu, Tzd, Tzu, xd, xu, yd, yu, zd, zu, old, A.sp);
                     } else {
                         // Octant selection (see the forward polish): lambda at a node depends on the
                         // neighbours with a larger traveltime.  Where on some axis only the neighbour
                         // visited after the node is larger, the node waits for its own sweep; where
                         // both are larger no sweep order has both fresh, and the node is updated.
-                        const unsigned m = adj_orders(dbits(t0), dbits(Txm), dbits(Txp), dbits(Tym), dbits(Typ),
-                                                      dbits(Tzm), dbits(Tzp));
+                        const unsigned m = adj_orders(dbits(t0), dbits(Txu), dbits(Txd), dbits(Tyu), dbits(Tyd),
+                                                      dbits(Tzu), dbits(Tzd));
                         sel |= m;
-                        if (m & obit) {
+                        if (m & 0x80u) {
                             bool big = false;
-                            nv = adj3_polish(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, box[c + 1], box[c - 1], box[c + HJ],
-                                             box[c - HJ], box[c + PS], box[c - PS], old, A.sp, A.polish_floor, big,
-                                             dstep);
+                            nv = adj3_polish(t0, Txd, Txu, Tyd, Tyu, Tzd, Tzu, xd, xu, yd, yu, zd, zu, old, A.sp,
+                                             A.polish_floor, big, dstep);
                             restep |= big;
                         }
                     }
@@ -652,28 +786,28 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                     if (fabsf(old - nv) > A.tol_abs_f + A.tol_rel_f * fabsf(nv)) moved = true;
                 }
                 if constexpr (kPrune) {
-                    // the neighbour node across a face (box index n, traveltime tn): does it
-                    // depend on this node?
-                    auto dep = [&](int n, Aux tn) {
+                    // does the neighbour across a face (value vn, traveltime tn) depend on this node?
+                    // The neighbour values were read before this step's stores, none of which
+                    // touches them (they lie on the hyperplanes t - 1 and t + 1).
+                    const long long lo = min(obits(old), obits(nv));
+                    auto dep = [&](Real vn, Aux tn) {
                         if constexpr (ADJ) return obits(t0) > obits(tn);
-                        else return min(obits(old), obits(nv)) < obits(box[n]);
+                        else return lo < obits(vn);
                     };
-                    if (lk == 0 && dep(c - PS, Tzm)) m_klo = true;
-                    if (lk == ek - 1 && dep(c + PS, Tzp)) m_khi = true;
-                    if (li == 0 && dep(c - HJ, Tym)) m_ilo = true;
-                    if (li == ei - 1 && dep(c + HJ, Typ)) m_ihi = true;
-                    if (lj == 0 && dep(c - 1, Txm)) chg_jlo = true;
-                    if (lj == ej - 1 && dep(c + 1, Txp)) chg_jhi = true;
+                    if (lkf == 0 && dep(zu, Tzu)) m_zu = true;
+                    if (lkf == ek - 1 && dep(zd, Tzd)) m_zd = true;
+                    if (lif == 0 && dep(yu, Tyu)) m_yu = true;
+                    if (lif == ei - 1 && dep(yd, Tyd)) m_yd = true;
+                    if (ljf == 0 && dep(xu, Txu)) m_xu = true;
+                    if (ljf == ej - 1 && dep(xd, Txd)) m_xd = true;
                     if constexpr (!kSelective) {
-                        // the in-tile neighbours this pass visited before the node (one step
-                        // back along each flipped axis)
-                        if (lkf > 0 && dep(pz ? c - PS : c + PS, pz ? Tzm : Tzp)) stale = true;
-                        if (lif > 0 && dep(py ? c - HJ : c + HJ, py ? Tym : Typ)) stale = true;
-                        if (ljf > 0 && dep(px ? c - 1 : c + 1, px ? Txm : Txp)) stale = true;
+                        // the in-tile neighbours this pass visited before the node (flipped upstream)
+                        if ((lkf > 0 && dep(zu, Tzu)) || (lif > 0 && dep(yu, Tyu)) || (ljf > 0 && dep(xu, Txu)))
+                            stale = true;
                     }
                 } else {
-                    if (lj == 0) chg_jlo = true;
-                    if (lj == ej - 1) chg_jhi = true;
+                    if (ljf == 0) m_xu = true;
+                    if (ljf == ej - 1) m_xd = true;
                 }
             }
         }
@@ -685,7 +819,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     }
 
     if constexpr (kSelective) {
-        const unsigned tsel = __reduce_or_sync(0xffffffffu, sel);
+        const unsigned tsel = xor_permute8(__reduce_or_sync(0xffffffffu, sel), ~dir & 7);
         dword = (dword & 0xff) | (int)(tsel << 8);
         if (lane == 0) dirty[tid] = dword;
     }
@@ -693,13 +827,16 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     // ---- nothing changed: the field and its snapshot comparison stand as they are
     if (!__any_sync(0xffffffffu, chg)) return;
 
-    // ---- unlock this tile and every face neighbour that sees a changed face node
-    const unsigned f_klo = __ballot_sync(0xffffffffu, kPrune ? m_klo : chg && lk == 0);
-    const unsigned f_khi = __ballot_sync(0xffffffffu, kPrune ? m_khi : chg && lk == ek - 1);
-    const unsigned f_ilo = __ballot_sync(0xffffffffu, kPrune ? m_ilo : chg && li == 0);
-    const unsigned f_ihi = __ballot_sync(0xffffffffu, kPrune ? m_ihi : chg && li == ei - 1);
-    const unsigned f_jlo = __ballot_sync(0xffffffffu, chg_jlo);
-    const unsigned f_jhi = __ballot_sync(0xffffffffu, chg_jhi);
+    // ---- unlock this tile and every face neighbour that sees a changed face node (flipped
+    // faces mapped back to grid faces)
+    const bool klo = kPrune ? (pz ? m_zu : m_zd) : chg && lk == 0, khi = kPrune ? (pz ? m_zd : m_zu) : chg && lk == ek - 1;
+    const bool ilo = kPrune ? (py ? m_yu : m_yd) : chg && li == 0, ihi = kPrune ? (py ? m_yd : m_yu) : chg && li == ei - 1;
+    const unsigned f_klo = __ballot_sync(0xffffffffu, klo);
+    const unsigned f_khi = __ballot_sync(0xffffffffu, khi);
+    const unsigned f_ilo = __ballot_sync(0xffffffffu, ilo);
+    const unsigned f_ihi = __ballot_sync(0xffffffffu, ihi);
+    const unsigned f_jlo = __ballot_sync(0xffffffffu, px ? m_xu : m_xd);
+    const unsigned f_jhi = __ballot_sync(0xffffffffu, px ? m_xd : m_xu);
     // Own re-marking.  A polish sweep in order o leaves every node that selects o consistent
     // with the values it reads (its active neighbours come before it in o), so after small
     // updates the tile is due again in o only when a neighbour or another order changes
@@ -724,11 +861,16 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
 
     // ---- write back; the FP64 kinds compare with the iteration-start snapshot
     if constexpr (!kSnap) {
+        if (A.vec_rows) {
+            store_tile_vec<Real>(fld, box, k0, i0, j0, ek, ei, ej, pz, py, px, nr, nc, lane);
+        } else {
 #pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
-            const int rk = m / TI, ri = m % TI;
-            if (rk < ek && ri < ei && lane < ej)
-                fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+            for (int m = 0; m < 32; ++m) {
+                const int rk = m / TI, ri = m % TI;
+                if (rk < ek && ri < ei && lane < ej)
+                    fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] =
+                        box[box_index(rk, ri, lane, ek, ei, ej, pz, py, px)];
+            }
         }
         if (__any_sync(0xffffffffu, moved) && lane == 0) A.diff[(long long)inst * A.ntiles + tid] = 1;
     } else {
@@ -745,7 +887,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             for (int u = 0; u < 8; ++u) {
                 const int m = m0 + u, rk = m / TI, ri = m % TI;
                 if (rk < ek && ri < ei && lane < ej) {
-                    const Real v = box[(rk + 1) * PS + (ri + 1) * HJ + lane + 1];
+                    const Real v = box[box_index(rk, ri, lane, ek, ei, ej, pz, py, px)];
                     fld[(k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane] = v;
                     if (fabs(p[u] - v) > A.tol_abs) moved = true;   // isconv, src/T_pfsm3d.h:126
                 }
