@@ -29,7 +29,7 @@ static_assert(TK * TI == 32, "one lane per (k,i) pencil");
 // (address = lk*(PS-1) + li*(HJ-1) + t with HJ-1 = 33 = 1 mod 32 and PS-1 = 8 mod 32).
 constexpr int HK = TK + 2, HI = TI + 2, HJ = TJ + 2, PS = 361;
 static_assert(PS >= HI * HJ && (PS - 1) % 32 == 8 && (HJ - 1) % 32 == 1, "bank-conflict-free stride");
-// Interior tile (slowness) layout: [TK][SPS] with rows of SJ.
+// Interior tile (the forward's staged slowness) layout, flipped like the box: [TK][SPS] with rows of SJ.
 constexpr int SJ = TJ + 2, SPS = 297;
 static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
 // Warps (tiles) per CTA.

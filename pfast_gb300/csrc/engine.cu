@@ -243,11 +243,12 @@ static pfast_status iteration_graph(pfast_ctx* ctx, const Sweep3Args& a, int kin
 }
 
 // Whether the tiles of a phase can move in 16-byte vectors: every grid row of the field (and of
-// the FP32 adjoint's staged traveltime) starts on a 16-byte boundary.
+// the staged auxiliary field: the forward's slowness, the FP32 adjoint's traveltime) starts on a
+// 16-byte boundary.
 static int rows_aligned(const Sweep3Args& a, int kind) {
     const int esz = (kind == kFwdFast32 || kind == kAdjFast32) ? 4 : 8;
     if (a.nc % (16 / esz) != 0 || reinterpret_cast<uintptr_t>(a.field) % 16 != 0) return 0;
-    if (kind == kAdjFast32 && reinterpret_cast<uintptr_t>(a.aux) % 16 != 0) return 0;
+    if (kind != kAdjPlain64 && kind != kAdjPolish64 && reinterpret_cast<uintptr_t>(a.aux) % 16 != 0) return 0;
     return 1;
 }
 

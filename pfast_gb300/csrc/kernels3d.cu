@@ -49,11 +49,24 @@ __host__ __device__ constexpr bool t_windows() {
 // Shared memory per warp: the field's halo box, plus the FP32 bulk adjoint's traveltime
 // box.  The forward's slowness is read per node through L1 (each lane walks its own row,
 // so a fetched line serves the next steps).
+// FP32 forward: the tile's slowness is staged in shared memory beside the box (interior tile,
+// flipped like the box), so that a wavefront step reads it there instead of issuing a global
+// load per node: with most of the SM's shared memory holding tile boxes, the L1 is too small to
+// keep the slowness lines of the resident tiles, and every such load went to L2 on the step's
+// dependency chain (3D gradient workload: FP32 forward 139 -> 116 ms per evaluation).  The FP64
+// kinds keep the per-node load: their staged tile (9.5 KB) would cost a third of the resident
+// warps, which was slower (forward polish 159 -> 197 ms).
+template <int KIND>
+__host__ __device__ constexpr bool stage_slowness() {
+    return KIND == kFwdFast32;
+}
+
 template <int KIND>
 __host__ __device__ constexpr int warp_smem_bytes() {
     using T = Traits<KIND>;
     return int(HK * PS * sizeof(typename T::Real) +
-               (T::adj && !t_windows<KIND>() ? HK * PS * sizeof(typename T::Aux) : 0));
+               (T::adj && !t_windows<KIND>() ? HK * PS * sizeof(typename T::Aux) : 0) +
+               (stage_slowness<KIND>() ? TK * SPS * sizeof(typename T::Aux) : 0));
 }
 
 
@@ -218,32 +231,38 @@ __device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, 
 }
 
 // FP32 bulk adjoint update (T as FP32 values; unreached nodes hold INF).  A change of
-// less than 2^-24 relative keeps the old value, so converged regions reach a bitwise
-// fixed point (rounding alone would otherwise keep flipping last bits).
-__device__ __forceinline__ float adj3_bulk(float T0, float Txp, float Txm, float Typ, float Tym, float Tzp, float Tzm,
-                                           float Lxp, float Lxm, float Lyp, float Lym, float Lzp, float Lzm, float L0,
+// less than 2^-24 relative keeps the old value, so converged regions reach a bitwise fixed
+// point (rounding alone would otherwise keep flipping last bits).  The two neighbours of an
+// axis enter as a commutative pair (two products, one sum) and the axes in a fixed order, so
+// the bits do not depend on which neighbour the sweep visits first: a node keeps one value
+// in all eight sweep orders once its neighbours have settled.
+__device__ __forceinline__ float adj3_bulk(float T0, float Ta, float Tb, float Tc, float Td, float Te, float Tf,
+                                           float La, float Lb, float Lc, float Ld, float Le, float Lf, float L0,
                                            const Spacing3& sp) {
     const float ti = (float)kInf;
-    if (T0 >= ti || Txp >= ti || Txm >= ti || Typ >= ti || Tym >= ti || Tzp >= ti || Tzm >= ti) return 0.f;
-    float e, den, num;
+    if (T0 >= ti || Ta >= ti || Tb >= ti || Tc >= ti || Td >= ti || Te >= ti || Tf >= ti) return 0.f;
+    // per axis: den = max(-e1, 0) + max(-e2, 0), num = max(e1, 0) L1 + max(e2, 0) L2
+    auto pair = [&](float T1, float L1, float T2, float L2, float& d, float& n) {
+        const float e1 = T1 - T0, e2 = T2 - T0;
+        d = fmaxf(-e1, 0.f) + fmaxf(-e2, 0.f);
+        const float p1 = fmaxf(e1, 0.f) * L1, p2 = fmaxf(e2, 0.f) * L2;
+        n = p1 + p2;
+    };
+    float dx, nx, dy, ny, dz, nz;
+    pair(Ta, La, Tb, Lb, dx, nx);   // x neighbours
+    pair(Tc, Lc, Td, Ld, dy, ny);   // y
+    pair(Te, Le, Tf, Lf, dz, nz);   // z
+    float den, num, r;
     if (sp.iso) {   // one weight: it cancels in num / den
-        e = Txp - T0; den = fmaxf(-e, 0.f); num = fmaxf(e, 0.f) * Lxp;
-        e = Txm - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lxm, num);
-        e = Typ - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lyp, num);
-        e = Tym - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lym, num);
-        e = Tzp - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lzp, num);
-        e = Tzm - T0; den += fmaxf(-e, 0.f); num = fmaf(fmaxf(e, 0.f), Lzm, num);
-        const float r = (den * sp.wf[0] > 1e-9f) ? __fdividef(num, den) : 0.f;
-        return fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r;
+        den = (dx + dy) + dz;
+        num = (nx + ny) + nz;
+        r = (den * sp.wf[0] > 1e-9f) ? __fdividef(num, den) : 0.f;
+    } else {
+        const float wx = sp.wf[0], wy = sp.wf[1], wz = sp.wf[2];
+        den = (wx * dx + wy * dy) + wz * dz;
+        num = (wx * nx + wy * ny) + wz * nz;
+        r = (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
     }
-    const float wx = sp.wf[0], wy = sp.wf[1], wz = sp.wf[2];
-    e = Txp - T0; den = wx * fmaxf(-e, 0.f); num = wx * fmaxf(e, 0.f) * Lxp;
-    e = Txm - T0; den = fmaf(wx, fmaxf(-e, 0.f), den); num = fmaf(wx * fmaxf(e, 0.f), Lxm, num);
-    e = Typ - T0; den = fmaf(wy, fmaxf(-e, 0.f), den); num = fmaf(wy * fmaxf(e, 0.f), Lyp, num);
-    e = Tym - T0; den = fmaf(wy, fmaxf(-e, 0.f), den); num = fmaf(wy * fmaxf(e, 0.f), Lym, num);
-    e = Tzp - T0; den = fmaf(wz, fmaxf(-e, 0.f), den); num = fmaf(wz * fmaxf(e, 0.f), Lzp, num);
-    e = Tzm - T0; den = fmaf(wz, fmaxf(-e, 0.f), den); num = fmaf(wz * fmaxf(e, 0.f), Lzm, num);
-    const float r = (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
     return fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r;
 }
 
@@ -431,6 +450,62 @@ __device__ __forceinline__ void store_tile_vec(T* __restrict__ fld, const T* box
     }
 }
 
+// The tile's interior values of a node field (the forward's slowness) into the warp's interior
+// tile, flipped like the box: node (kf, if, jf) at kf*SPS + if*SJ + jf, so that step t of lane
+// (kf, if) reads kf*(SPS-1) + if*(SJ-1) + t (SPS-1 = 8, SJ-1 = 1 mod 32: 32 distinct banks).
+// vec: 16-byte vector rows (same condition as load_box_vec), else one column per lane.
+template <typename T>
+__device__ __forceinline__ void load_interior(T* dst, const T* __restrict__ g, int k0, int i0, int j0, int ek, int ei,
+                                              int ej, bool pz, bool py, bool px, int nr, int nc, bool vec, int lane) {
+    const long long plane = (long long)nr * nc;
+    if (vec) {
+        using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+        constexpr int V = 16 / sizeof(T);
+        constexpr int MV = TJ / V, RPI = 32 / MV;
+        const int q = lane % MV, rsub = lane / MV;
+        const bool qok = q * V < ej;
+#pragma unroll 1
+        for (int r0 = 0; r0 < TK * TI; r0 += 4 * RPI) {
+            VT v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int r = r0 + u * RPI + rsub, rk = r / TI, ri = r - rk * TI;
+                if (qok && rk < ek && ri < ei)
+                    v[u] = __ldg(reinterpret_cast<const VT*>(g + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + q * V));
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int r = r0 + u * RPI + rsub, rk = r / TI, ri = r - rk * TI;
+                if (!(qok && rk < ek && ri < ei)) continue;
+                T* row = dst + (pz ? rk : ek - 1 - rk) * SPS + (py ? ri : ei - 1 - ri) * SJ;
+                const T* f = reinterpret_cast<const T*>(&v[u]);
+#pragma unroll
+                for (int e = 0; e < V; ++e) {
+                    const int rj = q * V + e;
+                    row[px ? rj : ej - 1 - rj] = f[e];
+                }
+            }
+        }
+    } else {
+        const int jf = px ? lane : ej - 1 - lane;
+#pragma unroll 1
+        for (int m0 = 0; m0 < TK * TI; m0 += 8) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int rk = (m0 + u) / TI, ri = (m0 + u) % TI;
+                if (rk < ek && ri < ei && lane < ej) v[u] = __ldg(g + (k0 + rk) * plane + (long long)(i0 + ri) * nc + j0 + lane);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int rk = (m0 + u) / TI, ri = (m0 + u) % TI;
+                if (rk < ek && ri < ei && lane < ej)
+                    dst[(pz ? rk : ek - 1 - rk) * SPS + (py ? ri : ei - 1 - ri) * SJ + jf] = v[u];
+            }
+        }
+    }
+}
+
 // Index of tile node (rk, ri, rj) (tile coordinates, grid orientation) in the flipped box.
 __device__ __forceinline__ int box_index(int rk, int ri, int rj, int ek, int ei, int ej, bool pz, bool py, bool px) {
     return ((pz ? rk : ek - 1 - rk) + 1) * PS + ((py ? ri : ei - 1 - ri) + 1) * HJ + (px ? rj : ej - 1 - rj) + 1;
@@ -569,6 +644,10 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     const Real fill = ADJ ? Real(0) : Real(INFINITY);
     if (A.vec_rows) load_box_vec<Real, COHERENT>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
     else load_box<Real, COHERENT>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
+    Aux* stile = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
+    if constexpr (stage_slowness<KIND>())
+        load_interior<Aux>(stile, reinterpret_cast<const Aux*>(A.aux), k0, i0, j0, ek, ei, ej, pz, py, px, nr, nc,
+                           A.vec_rows != 0, lane);
 
     // ---- auxiliary data
     unsigned fixed_bits = 0;   // adjoint: fixed nodes of this lane's pencil, bit jf (flipped position)
@@ -611,6 +690,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     const int steps = ek + ei + ej - 2;
     const int toff = lane_ok ? lkf + lif : (1 << 20);   // flipped column of step t: t - toff
     const int cl = (lkf + 1) * PS + (lif + 1) * HJ + 1 - lkf - lif;   // box index of step t: cl + t
+    const int sl = lkf * (SPS - 1) + lif * (SJ - 1);                   // staged slowness of step t: sl + t
     const int dj = px ? 1 : -1, gjA = j0 + (px ? 0 : ej - 1);      // grid column of jf: gjA + dj*jf
     int sk = -1, si = -1, sj = -1, qkqi = 0;
     bool near_src = false;   // forward: the tile meets the fixed region around the source
@@ -717,7 +797,9 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                 bool free_node = true;   // the source node (and the opt-in fixed region) stays
                 if (near_src) free_node = qkqi + (gj - sj) * (gj - sj) > A.src_r2;
                 if (free_node) {
-                    const Aux s = __ldg(srow + gj);
+                    Aux s;
+                    if constexpr (stage_slowness<KIND>()) s = stile[sl + t];
+                    else s = __ldg(srow + gj);
                     // the neighbour minima are symmetric in the two neighbours of an axis
                     if constexpr (KIND == kFwdPlain64) {
                         nv = min_nonneg(old, eik3_plain(min_nonneg(xd, xu), min_nonneg(yd, yu), min_nonneg(zd, zu), s, A.sp));
@@ -755,7 +837,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                         const Aux Tzp = pz ? Tzd : Tzu, Tzm = pz ? Tzu : Tzd;
                         nv = adj3_plain(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, A.sp);
                     } else if constexpr (KIND == kAdjFast32) {
-                        // each axis's two neighbours enter alike: flipped orientation (d for p, u for m)
+                        // the update is symmetric in the two neighbours of an axis
                         nv = adj3_bulk(t0, Txd, Txu, Tyd, Tyu, Tzd, Tzu, xd, xu, yd, yu, zd, zu, old, A.sp);
                     } else {
                         // Octant selection (see the forward polish): lambda at a node depends on the
@@ -766,8 +848,14 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                                                       dbits(Tzu), dbits(Tzd));
                         sel |= m;
                         if (m & 0x80u) {
+                            // the residual's FP64 sum in grid orientation (m: index - 1, p: index + 1),
+                            // the same in every sweep order
+                            const Real Lxp = px ? xd : xu, Lxm = px ? xu : xd, Lyp = py ? yd : yu, Lym = py ? yu : yd;
+                            const Real Lzp = pz ? zd : zu, Lzm = pz ? zu : zd;
+                            const Aux Txp = px ? Txd : Txu, Txm = px ? Txu : Txd, Typ = py ? Tyd : Tyu;
+                            const Aux Tym = py ? Tyu : Tyd, Tzp = pz ? Tzd : Tzu, Tzm = pz ? Tzu : Tzd;
                             bool big = false;
-                            nv = adj3_polish(t0, Txd, Txu, Tyd, Tyu, Tzd, Tzu, xd, xu, yd, yu, zd, zu, old, A.sp,
+                            nv = adj3_polish(t0, Txp, Txm, Typ, Tym, Tzp, Tzm, Lxp, Lxm, Lyp, Lym, Lzp, Lzm, old, A.sp,
                                              A.polish_floor, big, dstep);
                             restep |= big;
                         }
@@ -1078,11 +1166,12 @@ __device__ __forceinline__ void df_iteration(const Sweep3Args& A, const int inst
 }
 
 // Warps per block of the dataflow kernel, at most: what 227 KB of shared memory holds beside
-// the counters and ring of an 8192-tile grid (one FP32 box per warp for the FP32 forward, 17.3 KB
-// otherwise), so that the register budget of a thread follows the block size.
+// the counters and ring of an 8192-tile grid (24 at most), so that the register budget of a
+// thread follows the block size.
 template <int KIND>
 __host__ __device__ constexpr int df_max_warps() {
-    return warp_smem_bytes<KIND>() <= 9000 ? 22 : 11;
+    return (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND>() < 24 ? (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND>()
+                                                                       : 24;
 }
 
 template <int KIND>

@@ -270,6 +270,7 @@ def test_dataflow_schedule_matches_per_diagonal_on_many_tiles(ctx, shape, h):
         for k in ("fwd_iters_max", "adj_iters_max", "fwd32_iters_max", "adj32_iters_max", "fwd_node_updates",
                   "adj_node_updates", "not_converged"):
             assert a[3][k] == b[3][k], k
+        assert a[3]["not_converged"] == 0 and a[3]["adj32_iters_max"] < 20 and a[3]["fwd32_iters_max"] < 20
         assert b[3]["launches"] < a[3]["launches"]
     g0, e0, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h, nthreads=8)
     assert bits_equal(out[pg.PFAST_PLAIN_FP64, 2][0], g0) and out[pg.PFAST_PLAIN_FP64, 2][1] == e0
@@ -393,6 +394,7 @@ def test_full_size_grid(ctx):
     pp, _ = sv.forward(d, precision=pg.PFAST_PLAIN_FP64)
     gm, em, _ = sv.eval(d, precision=pg.PFAST_MIXED)
     gm1, em1, st1 = sv.eval(d, precision=pg.PFAST_MIXED, max_batch=1)
+    assert st1["not_converged"] == 0 and st1["adj32_iters_max"] < 20 and st1["adj_iters_max"] < 20
     pm, _ = sv.forward(d, precision=pg.PFAST_MIXED)
     sv.close()
     gp, gm, pp, pm = gp.cpu().numpy(), gm.cpu().numpy(), pp.cpu().numpy(), pm.cpu().numpy()
