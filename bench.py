@@ -194,13 +194,13 @@ def run_reference(args, rank):
 def extras():
     """Secondary workloads, each reported beside the headline (bounded: about two minutes in all):
     the 2D joint inversion (15 L-BFGS iterations, mixed vs plain FP64), 48 uneven 3D models
-    batched through the request server vs sequential plain FP64 (plain timed on 12 models and
-    scaled), and a Poisson serving stream swept over offered loads until p99 latency degrades
+    in one batched evaluation (mixed and plain) vs sequential plain FP64 and vs the request
+    server, and a Poisson serving stream swept over offered loads until p99 latency degrades
     (mixed 4-128 requests/s, plain 1-4 requests/s)."""
     out = {}
     jobs = (("inversion_2d", lambda: __import__("pfast_gb300.inv_bench", fromlist=["run"]).run(15)),
             ("batched_uneven_3d", lambda: {k: v for k, v in __import__("pfast_gb300.batch_bench", fromlist=["run"])
-                                           .run(48, 8, plain_models=12).items() if k not in ("shapes", "sources")}),
+                                           .run(48, 8).items() if k not in ("shapes", "sources")}),
             ("serving", serving))
     for key, fn in jobs:
         try:

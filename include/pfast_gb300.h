@@ -152,6 +152,18 @@ pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const do
 pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
                                      pfast_stats* stats_diagonal, pfast_stats* stats_persistent);
 
+/* Misfit + gradient of n independent (model, survey) pairs at once: the reference's per-model
+ * evaluation (the source loop of src/T_PFAST3D.cpp:387-399, one model per run) for many models
+ * of different grids.  Every sweep phase of all pairs runs as one dataflow launch over their
+ * (model, source) instances, largest grid first, each instance retiring as it converges; the
+ * steps between phases run per model.  Each pair's gradient, misfit and iteration counts equal
+ * those of pfast_survey3d_eval on it alone (schedule and max_batch of opt are not used).
+ * surveys[m] (of this context, with picks), vp[m] and grad[m] (DEVICE arrays of that grid's
+ * size); misfit: HOST [n]; stats: summed over the pairs (optional).  Grids of at most 8192
+ * tiles of 4x8x32 nodes; pairs are grouped to fit the device memory. */
+pfast_status pfast_surveys3d_eval(pfast_ctx* ctx, int n, pfast_survey3d* const* surveys, const double* const* vp,
+                                  double* const* grad, double* misfit, const pfast_options* opt, pfast_stats* stats);
+
 /* One-call host-buffer forms (copies in and out inside the call). */
 pfast_status pfast_eval3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols, int nz, double dx, double dy,
                           double dz, int nsrc, const int* src, const int* srnum, const int* rec, const double* nxyz,

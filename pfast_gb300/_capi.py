@@ -131,6 +131,7 @@ SIGNATURES = [
     ("pfast_survey3d_eval", _i, [_p, _p, _p, _p, _p, _p, _p]),
     ("pfast_survey3d_forward", _i, [_p, _p, _p, _p, _p, _p]),
     ("pfast_survey3d_autotune", _i, [_p, _p, _p, _p, _p, _p]),
+    ("pfast_surveys3d_eval", _i, [_p, _i, _p, _p, _p, _p, _p, _p]),
     ("pfast_eval3d", _i, [_p, _p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     ("pfast_forward3d", _i, [_p, _p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p]),
     ("pfast_survey2d_create", _i, [_p, _i, _i, _d, _d, _i, _p, _p, _i, _p, _p, _p, _i, _p, _p, _p]),

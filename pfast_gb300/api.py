@@ -21,7 +21,7 @@ from . import _capi
 from ._capi import PFAST_MIXED, PFAST_PLAIN_FP64, PfastError, check, lib
 
 __all__ = ["fsm3d", "adjoint_fsm3d", "RT_fsm2d", "Tadjoint_fsm2d", "Radjoint_fsm2d", "Context", "Survey3D",
-           "Survey2D", "eval3d_host", "forward3d_host", "Inversion", "invert_options", "Server", "Ticket", "PfastError",
+           "Survey2D", "eval3d_many", "eval3d_host", "forward3d_host", "Inversion", "invert_options", "Server", "Ticket", "PfastError",
            "PFAST_PLAIN_FP64", "PFAST_MIXED"]
 
 
@@ -288,6 +288,29 @@ class Survey2D:
             self.close()
         except Exception:
             pass
+
+
+def eval3d_many(ctx, surveys, vps, grads=None, precision=PFAST_PLAIN_FP64, maxswp=100, polish_floor=0.0,
+                near_source_radius=0):
+    """Misfit + gradient of many (Survey3D, device model) pairs at once (pfast_surveys3d_eval):
+    every sweep phase of all pairs runs as one dataflow launch over their (model, source)
+    instances.  Each pair's results equal Survey3D.eval on it alone.  Returns (list of gradient
+    tensors, list of misfits, summed stats dict)."""
+    import torch
+    n = len(surveys)
+    if len(vps) != n:
+        raise ValueError("one model per survey")
+    if grads is None:
+        grads = [torch.empty(sv.shape, dtype=torch.float64, device=vp.device) for sv, vp in zip(surveys, vps)]
+    hs = (C.c_void_p * max(n, 1))(*[sv._h.value for sv in surveys])
+    vs = (C.c_void_p * max(n, 1))(*[_dev_ptr(vp, "vp", numel=int(np.prod(sv.shape))) for sv, vp in zip(surveys, vps)])
+    gs = (C.c_void_p * max(n, 1))(*[_dev_ptr(g, "grad", numel=int(np.prod(sv.shape))) for sv, g in zip(surveys, grads)])
+    E = np.zeros(max(n, 1))
+    st = _capi.Stats()
+    o = _opts(precision, maxswp, 0, polish_floor, 0, near_source_radius)
+    check(lib().pfast_surveys3d_eval(ctx.handle, n, C.addressof(hs), C.addressof(vs), C.addressof(gs), E.ctypes.data,
+                                     C.byref(o), C.byref(st)), "surveys3d_eval")
+    return grads, [float(e) for e in E[:n]], st.as_dict()
 
 
 def eval3d_host(ctx, vp, dx, dy, dz, src, srnum, rec, nxyz, tobs, precision=PFAST_PLAIN_FP64, maxswp=100,

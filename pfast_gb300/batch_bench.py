@@ -10,11 +10,12 @@ largest size), 4-128 surface sources each (uniform integer), receivers on every 
 node, picks from the true model plus 2 ms noise; every instance evaluates misfit + gradient
 on the 1D starting model once.
 
-Batched: all instances submitted at once to the request server (`slots` running at a time on
-their own streams, each solving all of its sources in one batch), mixed precision.
-Baseline: the same evaluations one model after another with the plain FP64 path (the
-per-model launches of the reference-equivalent arithmetic).  Reports both wall times,
-models/s, and the largest gradient difference between the two paths.
+Batched: all models in one evaluation (pfast_surveys3d_eval): every sweep phase runs as one
+dataflow launch over all (model, source) instances, largest grid first, each retiring as it
+converges; in mixed precision and in plain FP64, so that the gains of batching and of precision
+show separately.  Baseline: the same evaluations one model after another with the plain FP64
+path.  Also the request-server path (`slots` models at a time on their own streams).  Reports
+wall times, models/s, and the largest gradient difference between mixed and plain.
 """
 import argparse
 import json
@@ -64,7 +65,10 @@ def observed(ctx, inst):
     return synth.add_noise(pk.cpu().numpy(), 0.002, inst["seed"])
 
 
-def run(n_models=48, slots=8, budget_gb=150.0, plain_models=None):
+def run(n_models=48, slots=8, budget_gb=150.0, plain_models=None, server=True):
+    """Batched (one dataflow launch per sweep phase over all models' sources, pfast_surveys3d_eval)
+    in mixed precision and in plain FP64, the sequential per-model plain FP64 baseline, and the
+    request-server path (slots models at a time on their own streams)."""
     import torch
     import pfast_gb300 as pg
     insts = instances(n_models)
@@ -72,46 +76,64 @@ def run(n_models=48, slots=8, budget_gb=150.0, plain_models=None):
     for inst in insts:
         inst["tobs"] = observed(ctx, inst)
     node_src = sum(int(np.prod(i["shape"])) * len(i["srnum"]) for i in insts)
-    # batched, mixed precision, through the server
-    srv = pg.Server(slots=slots, hbm_budget_gb=budget_gb)
-    for k, inst in enumerate(insts):
-        srv.put_model(k, inst["start"], (H, H, H))
-        srv.put_survey3d(k, inst["shape"], (H, H, H), inst["src"], inst["srnum"], inst["rec"], inst["nxyz"],
-                         inst["tobs"])
-    # warm-up on the smallest instance (tables, allocations)
-    small = min(range(n_models), key=lambda k: np.prod(insts[k]["shape"]))
-    srv.submit_gradient(small, small).result()
-    t0 = time.perf_counter()
-    tickets = [srv.submit_gradient(k, k, pg.PFAST_MIXED) for k in range(n_models)]
-    res = [t.result() for t in tickets]
-    t_batched = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    # sequential plain FP64 per model (direct survey API, inputs resident)
-    m_plain = n_models if plain_models is None else min(plain_models, n_models)
-    t_plain = 0.0
-    max_rel = 0.0
-    for k in range(m_plain):
-        inst = insts[k]
-        nz, nr, nc = inst["shape"]
-        sv = pg.Survey3D(ctx, nr, nc, nz, H, H, H, inst["src"], inst["srnum"], inst["rec"], inst["nxyz"], inst["tobs"])
-        d = torch.from_numpy(inst["start"]).cuda()
+    svs = [pg.Survey3D(ctx, i["shape"][1], i["shape"][2], i["shape"][0], H, H, H, i["src"], i["srnum"], i["rec"],
+                       i["nxyz"], i["tobs"]) for i in insts]
+    vps = [torch.from_numpy(i["start"]).cuda() for i in insts]
+    out = {"models": n_models, "node_sources": node_src}
+
+    def timed(fn):
         torch.cuda.synchronize()
         a = time.perf_counter()
-        g, e, _ = sv.eval(d, precision=pg.PFAST_PLAIN_FP64)
+        r = fn()
         torch.cuda.synchronize()
-        t_plain += time.perf_counter() - a
-        gp = g.cpu().numpy()
-        max_rel = max(max_rel, float(np.linalg.norm(res[k][0] - gp) / np.linalg.norm(gp)))
-        sv.close()
-    ctx.close()
+        return r, time.perf_counter() - a
+
+    # batched: all models in one evaluation (a warm-up call first: kernel attributes, buffers)
+    pg.eval3d_many(ctx, svs[:2], vps[:2], precision=pg.PFAST_MIXED)
+    (gm, em, stm), t_bm = timed(lambda: pg.eval3d_many(ctx, svs, vps, precision=pg.PFAST_MIXED))
+    gm = [g.cpu().numpy() for g in gm]
+    (gp, ep, stp), t_bp = timed(lambda: pg.eval3d_many(ctx, svs, vps, precision=pg.PFAST_PLAIN_FP64))
+    gp = [g.cpu().numpy() for g in gp]
+    out.update({"batched_mixed_s": t_bm, "batched_mixed_models_per_s": n_models / t_bm,
+                "batched_mixed_launches": stm["launches"], "batched_mixed_not_converged": stm["not_converged"],
+                "batched_plain_s": t_bp, "batched_plain_models_per_s": n_models / t_bp,
+                "grad_rel_l2_max_mixed_vs_plain": max(float(np.linalg.norm(a - b) / np.linalg.norm(b))
+                                                      for a, b in zip(gm, gp))})
+    # sequential plain FP64, one model after another (direct survey API, inputs resident)
+    m_plain = n_models if plain_models is None else min(plain_models, n_models)
+    t_plain = 0.0
+    max_diff = 0.0
+    for k in range(m_plain):
+        (g, e, _), t = timed(lambda: svs[k].eval(vps[k], precision=pg.PFAST_PLAIN_FP64))
+        t_plain += t
+        max_diff = max(max_diff, float(np.abs(g.cpu().numpy() - gp[k]).max()))
     plain_scaled = t_plain * n_models / m_plain
-    return {"models": n_models, "node_sources": node_src, "slots": slots,
-            "batched_mixed_s": t_batched, "batched_models_per_s": n_models / t_batched,
-            "sequential_plain_s": plain_scaled, "sequential_plain_models_per_s": n_models / plain_scaled,
-            "plain_sample_models": m_plain, "speedup": plain_scaled / t_batched,
-            "grad_rel_l2_max": max_rel, "peak_gb": st["peak_bytes"] / 1e9,
-            "shapes": [list(i["shape"]) for i in insts], "sources": [len(i["srnum"]) for i in insts]}
+    out.update({"sequential_plain_s": plain_scaled, "sequential_plain_models_per_s": n_models / plain_scaled,
+                "plain_sample_models": m_plain, "batched_plain_equals_sequential": max_diff == 0.0,
+                "speedup_batched_mixed_vs_sequential_plain": plain_scaled / t_bm,
+                "speedup_batching_plain": plain_scaled / t_bp, "speedup_precision_batched": t_bp / t_bm})
+    for sv in svs:
+        sv.close()
+    if server:
+        srv = pg.Server(slots=slots, hbm_budget_gb=budget_gb)
+        for k, inst in enumerate(insts):
+            srv.put_model(k, inst["start"], (H, H, H))
+            srv.put_survey3d(k, inst["shape"], (H, H, H), inst["src"], inst["srnum"], inst["rec"], inst["nxyz"],
+                             inst["tobs"])
+        small = min(range(n_models), key=lambda k: np.prod(insts[k]["shape"]))
+        srv.submit_gradient(small, small).result()
+        t0 = time.perf_counter()
+        tickets = [srv.submit_gradient(k, k, pg.PFAST_MIXED) for k in range(n_models)]
+        for t in tickets:
+            t.result()
+        out["server_mixed_s"] = time.perf_counter() - t0
+        out["server_slots"] = slots
+        out["server_peak_gb"] = srv.stats()["peak_bytes"] / 1e9
+        srv.close()
+    ctx.close()
+    out["shapes"] = [list(i["shape"]) for i in insts]
+    out["sources"] = [len(i["srnum"]) for i in insts]
+    return out
 
 
 def main():

@@ -86,7 +86,7 @@ std::vector<DevBuf*> ctx_buffers(pfast_ctx* ctx) {
     return {&ctx->s64,  &ctx->s32,  &ctx->sq64,     &ctx->T32,    &ctx->tflags,    &ctx->T64,   &ctx->L64,
             &ctx->scratch, &ctx->mask, &ctx->act,  &ctx->changed, &ctx->ee,     &ctx->need,    &ctx->misc,
             &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a, &ctx->f2b, &ctx->f2c, &ctx->work,
-            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c, &ctx->dyn};
+            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c, &ctx->dyn, &ctx->multi, &ctx->multi_meta};
 }
 
 void ctx_release_buffers(pfast_ctx* ctx) {
@@ -133,8 +133,6 @@ namespace {
 
 // FP32 bulk phases stop once no node moves by more than ~8 ulps (relative);
 // FP64 phases use the reference's absolute 1e-9.
-constexpr double kTol32Rel = 1.0 / (1 << 20);
-constexpr double kTol32AbsAdj = 1e-6;
 
 Spacing3 make_spacing(double dx, double dy, double dz) {
     Spacing3 s;
@@ -245,7 +243,7 @@ static pfast_status iteration_graph(pfast_ctx* ctx, const Sweep3Args& a, int kin
 // Whether the tiles of a phase can move in 16-byte vectors: every grid row of the field (and of
 // the staged auxiliary field: the forward's slowness, the FP32 adjoint's traveltime) starts on a
 // 16-byte boundary.
-static int rows_aligned(const Sweep3Args& a, int kind) {
+int rows_aligned_impl(const Sweep3Args& a, int kind) {
     const int esz = (kind == kFwdFast32 || kind == kAdjFast32) ? 4 : 8;
     if (a.nc % (16 / esz) != 0 || reinterpret_cast<uintptr_t>(a.field) % 16 != 0) return 0;
     if (kind != kAdjPlain64 && kind != kAdjPolish64 && reinterpret_cast<uintptr_t>(a.aux) % 16 != 0) return 0;
@@ -255,7 +253,7 @@ static int rows_aligned(const Sweep3Args& a, int kind) {
 pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable3& dt, int nb,
                          std::vector<int>& active, int maxiter, int* iters, long long nodes_per_sweep,
                          long long* node_updates, int* not_conv, double* ms_acc) {
-    a.vec_rows = rows_aligned(a, kind);
+    a.vec_rows = rows_aligned_impl(a, kind);
     PFAST_TRY(ctx->act.ensure(sizeof(int) * nb));
     PFAST_TRY(ctx->changed.ensure(sizeof(int) * nb));
     PFAST_TRY(ctx->h_act.ensure(sizeof(int) * nb));
@@ -401,7 +399,7 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     return PFAST_OK;
 }
 
-Sweep3Args base_args(const pfast_survey3d* sv) {
+Sweep3Args base_args_impl(const pfast_survey3d* sv) {
     Sweep3Args a;
     std::memset(&a, 0, sizeof(a));
     a.nz = sv->nz;
@@ -446,7 +444,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     PFAST_TRY(ctx->T64.ensure(sizeof(double) * N * nb));
     PFAST_TRY(ctx->scratch.ensure(sizeof(double) * N * nb));
     std::vector<int> iters(nb, 0), active(nb);
-    Sweep3Args a = base_args(sv);
+    Sweep3Args a = base_args_impl(sv);
     a.fstride = N;
     a.src_kij = sv->d_src_kij + 3 * b0;
     a.src_r2 = ctx->near_radius * ctx->near_radius;
@@ -564,7 +562,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         if (ctx->h_need.as<int>()[b]) active.push_back(b);
     const long long interior =
         (long long)std::max(0, sv->nz - 2) * std::max(0, sv->nr - 2) * std::max(0, sv->nc - 2);
-    Sweep3Args a = base_args(sv);
+    Sweep3Args a = base_args_impl(sv);
     a.fstride = N;
     a.mask = ctx->mask.as<unsigned>();
     a.mask_stride = mwords;
@@ -620,7 +618,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
 
 namespace {
 
-bool valid_options(const pfast_options* opt) {
+bool valid_options_impl(const pfast_options* opt) {
     if (!opt) return true;
     if (opt->precision != PFAST_PLAIN_FP64 && opt->precision != PFAST_MIXED) {
         set_last_error("unknown precision %d", opt->precision);
@@ -645,7 +643,7 @@ bool valid_options(const pfast_options* opt) {
     return true;
 }
 
-pfast_options resolve(const pfast_options* opt, int default_maxswp) {
+pfast_options resolve_impl(const pfast_options* opt, int default_maxswp) {
     pfast_options o;
     o.precision = PFAST_PLAIN_FP64;
     o.maxswp = default_maxswp;
@@ -669,11 +667,17 @@ int pick_batch(int nsrc, int max_batch, size_t bytes_per_src) {
     return std::max(1, std::min(b, 65535));
 }
 
-void stats_begin(pfast_stats* st) {
+void stats_begin_impl(pfast_stats* st) {
     if (st) std::memset(st, 0, sizeof(*st));
 }
 
 }  // namespace
+
+Sweep3Args survey_sweep_args(const pfast_survey3d* sv) { return base_args_impl(sv); }
+int rows_aligned(const Sweep3Args& a, int kind) { return rows_aligned_impl(a, kind); }
+bool valid_options(const pfast_options* opt) { return valid_options_impl(opt); }
+pfast_options resolve_options(const pfast_options* opt, int default_maxswp) { return resolve_impl(opt, default_maxswp); }
+void stats_begin(pfast_stats* st) { stats_begin_impl(st); }
 
 }  // namespace pfast
 
@@ -862,14 +866,14 @@ pfast_status pfast_survey3d_destroy(pfast_survey3d* sv) {
 static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
                                  double* grad, double* misfit, double* picks, pfast_stats* stats) {
     if (!ctx || !sv || !vp) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
-    if (!valid_options(opt)) return PFAST_ERR_INVALID;
+    if (!valid_options_impl(opt)) return PFAST_ERR_INVALID;
     const bool want_grad = grad != nullptr;
     if (want_grad && !sv->has_picks) { set_last_error("survey has no picks: gradient unavailable"); return PFAST_ERR_INVALID; }
-    pfast_options o = resolve(opt, 100);
+    pfast_options o = resolve_impl(opt, 100);
     ctx->polish_floor = o.polish_floor > 0.0 ? (float)o.polish_floor : kPolishFloor;
     ctx->schedule = o.schedule;
     ctx->near_radius = o.near_source_radius;
-    stats_begin(stats);
+    stats_begin_impl(stats);
     PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
     cudaStream_t s = ctx->stream;
@@ -922,10 +926,10 @@ pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const do
 pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
                                      pfast_stats* stats_diagonal, pfast_stats* stats_persistent) {
     if (!ctx || !sv || !vp) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
-    if (!valid_options(opt)) return PFAST_ERR_INVALID;
+    if (!valid_options_impl(opt)) return PFAST_ERR_INVALID;
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
     PFAST_TRY(ctx->out_a.ensure(sizeof(double) * std::max<long long>(N, sv->nrec)));
-    pfast_options o = resolve(opt, 100);
+    pfast_options o = resolve_impl(opt, 100);
     pfast_stats* sts[2] = {stats_diagonal, stats_persistent};
     ctx->tuning = true;
     pfast_status r = PFAST_OK;

@@ -53,6 +53,8 @@ struct pfast_ctx {
     pfast::DevBuf queue;                // work counter of the persistent sweep kernel
     pfast::DevBuf out_a, out_b, out_c;  // request server: device outputs of a request
     pfast::DevBuf dyn;                  // replayed iteration graphs: outer iteration, active instances
+    pfast::DevBuf multi;                // multi-model evaluations: the models' work arrays
+    pfast::DevBuf multi_meta;           // multi-model evaluations: argument table and instance list
     pfast::HostBuf h_dyn;
     // One outer iteration of a per-diagonal phase as an instantiated CUDA graph, keyed by the
     // sweep kind, the launch arguments and the active-instance count it was captured with.
@@ -173,6 +175,18 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
 // Adjoint for the same batch (T in ctx->T64): lambda into ctx->L64, EE per source into ee_out.
 pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, int nb, int precision, int maxswp,
                              double* ee_out, pfast_stats* st);
+
+// FP32 bulk phases stop once no node moves by more than ~8 ulps (relative; the adjoint also
+// 1e-6 absolute); FP64 phases use the reference's absolute 1e-9.
+constexpr double kTol32Rel = 1.0 / (1 << 20);
+constexpr double kTol32AbsAdj = 1e-6;
+// Sweep arguments common to every phase of a survey's evaluation (grid, spacing, floor).
+Sweep3Args survey_sweep_args(const pfast_survey3d* sv);
+// Whether a phase's tiles can move in 16-byte vectors (Sweep3Args::vec_rows).
+int rows_aligned(const Sweep3Args& a, int kind);
+bool valid_options(const pfast_options* opt);
+pfast_options resolve_options(const pfast_options* opt, int default_maxswp);
+void stats_begin(pfast_stats* st);
 
 // 2D pipelines (engine2d.cu).
 pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, const pfast_options* opt,

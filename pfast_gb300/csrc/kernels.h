@@ -86,9 +86,16 @@ pfast_status launch_sweep3(int kind, const Sweep3Args& a, int d0, int tiles, int
 // a.stamp as for the per-diagonal launches; a.ntiles <= kDataflowMaxTiles.
 pfast_status launch_sweep3_dataflow(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
                                     int warps, int blocks, cudaStream_t st);
+// The dataflow kernel over instances of several grids: item q is instance items[q].y of the grid
+// whose arguments are models[items[q].x] (a device array; each model's result goes to its own
+// `changed` array); max_ntiles: the largest grid's tile count (<= kDataflowMaxTiles); warps and
+// blocks from dataflow_shape(kind, max_ntiles, nitems, warps, blocks, true).
+pfast_status launch_sweep3_dataflow_multi(int kind, const Sweep3Args* models, const int2* items, int nitems,
+                                          int max_ntiles, int maxiter, int* queue, int warps, int blocks,
+                                          cudaStream_t st);
 // Warps per block (as many as shared memory holds) and resident blocks
 // of the dataflow kernel; *warps = 0 when a grid of ntiles tiles does not fit.
-pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks);
+pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks, bool multi = false);
 
 // Small 3D kernels.
 // s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64*sq_scale (if non-null); *bad is set

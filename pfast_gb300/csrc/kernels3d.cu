@@ -17,6 +17,7 @@
 // step in FP32, so the fixed point is the FP64 one while FP64 issue slots (about 2
 // lanes per clock per SM on this part) go only where the precision is needed.
 
+#include <cstring>
 #include <map>
 #include <tuple>
 #include <mutex>
@@ -1035,6 +1036,9 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
 // progress for two seconds sets *err, records the instance as not converged and exits.
 // result[inst] = iterations | 1 << 30 when not converged.
 constexpr unsigned kSlotEmpty = 0xffffffffu;
+// shared-memory copy of a model's arguments (multi-grid launches)
+constexpr int kDfArgsBytes = (int)((sizeof(Sweep3Args) + 15) / 16 * 16);
+static_assert(sizeof(Sweep3Args) % 8 == 0 && sizeof(Sweep3Args) % 4 == 0, "argument copy by words");
 
 struct DataflowShared {
     unsigned head, tail;   // ring positions: next to take / next to fill
@@ -1174,8 +1178,14 @@ __host__ __device__ constexpr int df_max_warps() {
                                                                        : 24;
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(df_max_warps<KIND>() * 32, 1) sweep3d_dataflow(const Sweep3Args A, const int nact,
+// MULTI: instances of several grids in one launch.  Item q of the queue is models[items[q].x]'s
+// instance items[q].y; the block copies that model's arguments into shared memory when it takes
+// the item, and the result goes to the model's `changed` array.  Otherwise the instances are
+// A.act[q] of the one grid in A and results go to result[].
+template <int KIND, bool MULTI>
+__global__ void __launch_bounds__(df_max_warps<KIND>() * 32, 1) sweep3d_dataflow(const Sweep3Args A0,
+                                                                      const Sweep3Args* __restrict__ models,
+                                                                      const int2* __restrict__ items, const int nact,
                                                                       const int maxiter, int* __restrict__ queue,
                                                                       int* __restrict__ result, const int qcap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1184,18 +1194,36 @@ __global__ void __launch_bounds__(df_max_warps<KIND>() * 32, 1) sweep3d_dataflow
     const int nthr = blockDim.x, nw = nthr >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* wsm = smem_raw + warp * warp_smem_bytes<KIND>();
-    const int ntiles = A.ntiles, ncw = (ntiles + 3) >> 2;
-    unsigned* cnt = reinterpret_cast<unsigned*>(smem_raw + nw * warp_smem_bytes<KIND>());
-    unsigned* slots = cnt + ncw;
+    // after the warps' boxes: (MULTI: the current model's arguments,) the counters, the ring
+    unsigned char* dyn = smem_raw + nw * warp_smem_bytes<KIND>();
+    Sweep3Args& s_args = *reinterpret_cast<Sweep3Args*>(dyn);
+    unsigned* cnt = reinterpret_cast<unsigned*>(dyn + (MULTI ? kDfArgsBytes : 0));
     const unsigned qmask = (unsigned)qcap - 1u;
-    const TileGrid3 g{A.nbk, A.nbi, A.nbj};
+    int cur_model = -1;
     for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(queue, 1);
         __syncthreads();
         const int item = sh.item;
         __syncthreads();
         if (item >= nact) return;   // block-uniform
-        const int inst = A.act[item];
+        int inst;
+        if constexpr (MULTI) {
+            const int2 mi = items[item];
+            if (mi.x != cur_model) {   // block-uniform
+                const int* srcw = reinterpret_cast<const int*>(models + mi.x);
+                int* dstw = reinterpret_cast<int*>(&s_args);
+                for (int w = threadIdx.x; w < (int)(sizeof(Sweep3Args) / 4); w += nthr) dstw[w] = srcw[w];
+                cur_model = mi.x;
+                __syncthreads();
+            }
+            inst = mi.y;
+        } else {
+            inst = A0.act[item];
+        }
+        const Sweep3Args& A = MULTI ? s_args : A0;
+        const int ntiles = A.ntiles, ncw = (ntiles + 3) >> 2;
+        unsigned* slots = cnt + ncw;
+        const TileGrid3 g{A.nbk, A.nbi, A.nbj};
         int* diff = A.diff + (long long)inst * ntiles;
         const int* dirty = A.dirty + (long long)inst * ntiles;
         int it = 0;
@@ -1239,7 +1267,10 @@ __global__ void __launch_bounds__(df_max_warps<KIND>() * 32, 1) sweep3d_dataflow
             // change nothing and pass the test; it is counted without running
             if (!due && it < maxiter) { ++it; moved = false; break; }
         }
-        if (threadIdx.x == 0) result[inst] = it | (moved ? (1 << 30) : 0) | (aborted ? (1 << 29) : 0);
+        if (threadIdx.x == 0) {
+            int* res = MULTI ? A.changed : result;
+            res[inst] = it | (moved ? (1 << 30) : 0) | (aborted ? (1 << 29) : 0);
+        }
         if (aborted) {
             if (threadIdx.x == 0) atomicOr(queue + 1, 1);   // the host reports the stall
             return;                                        // block-uniform
@@ -1423,19 +1454,19 @@ static int dataflow_qcap(int ntiles) {
     return q;
 }
 
-static size_t dataflow_extra_bytes(int ntiles) {
-    return (size_t)4 * ((ntiles + 3) / 4) + (size_t)4 * dataflow_qcap(ntiles);
+static size_t dataflow_extra_bytes(int ntiles, bool multi) {
+    return (size_t)4 * ((ntiles + 3) / 4) + (size_t)4 * dataflow_qcap(ntiles) + (multi ? kDfArgsBytes : 0);
 }
 
 template <int KIND>
-static pfast_status dataflow_shape_k(int ntiles, int nact, int* warps, int* blocks) {
-    static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;   // (device, ntiles, nact)
+static pfast_status dataflow_shape_k(int ntiles, int nact, bool multi, int* warps, int* blocks) {
+    static std::map<std::tuple<int, int, int, bool>, std::pair<int, int>> cache;   // (device, ntiles, nact, multi)
     static std::mutex mu;
     int dev = 0, sms = 0, smem_max = 0;
     PFAST_CUDA_TRY(cudaGetDevice(&dev));
     {
         std::lock_guard<std::mutex> lk(mu);
-        auto it = cache.find(std::make_tuple(dev, ntiles, nact));
+        auto it = cache.find(std::make_tuple(dev, ntiles, nact, multi));
         if (it != cache.end()) {
             *warps = it->second.first;
             *blocks = it->second.second;
@@ -1444,42 +1475,77 @@ static pfast_status dataflow_shape_k(int ntiles, int nact, int* warps, int* bloc
     }
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const long long room = (long long)smem_max - 256 - (long long)dataflow_extra_bytes(ntiles);
+    const long long room = (long long)smem_max - 256 - (long long)dataflow_extra_bytes(ntiles, multi);
     const int w = (int)std::min<long long>(df_max_warps<KIND>(), room / warp_smem_bytes<KIND>());
     if (ntiles > kDataflowMaxTiles || w < 1) {
         *warps = 0;
         *blocks = 0;
         return PFAST_OK;
     }
-    const size_t smem = (size_t)w * warp_smem_bytes<KIND>() + dataflow_extra_bytes(ntiles);
-    PFAST_CUDA_TRY(cudaFuncSetAttribute(sweep3d_dataflow<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = (size_t)w * warp_smem_bytes<KIND>() + dataflow_extra_bytes(ntiles, multi);
+    auto fn = multi ? sweep3d_dataflow<KIND, true> : sweep3d_dataflow<KIND, false>;
+    PFAST_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    PFAST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep3d_dataflow<KIND>, w * 32, smem));
+    PFAST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, w * 32, smem));
     *warps = w;
     *blocks = std::max(1, std::min(nact, std::max(1, per_sm) * sms));
     std::lock_guard<std::mutex> lk(mu);
-    cache[std::make_tuple(dev, ntiles, nact)] = {*warps, *blocks};
+    cache[std::make_tuple(dev, ntiles, nact, multi)] = {*warps, *blocks};
     return PFAST_OK;
 }
 
 template <int KIND>
 static pfast_status launch_dataflow_k(const Sweep3Args& a, int nact, int maxiter, int* queue, int* result, int warps,
                                       int blocks, cudaStream_t st) {
-    const size_t smem = (size_t)warps * warp_smem_bytes<KIND>() + dataflow_extra_bytes(a.ntiles);
-    sweep3d_dataflow<KIND><<<blocks, warps * 32, smem, st>>>(a, nact, maxiter, queue, result, dataflow_qcap(a.ntiles));
+    const size_t smem = (size_t)warps * warp_smem_bytes<KIND>() + dataflow_extra_bytes(a.ntiles, false);
+    sweep3d_dataflow<KIND, false><<<blocks, warps * 32, smem, st>>>(a, nullptr, nullptr, nact, maxiter, queue, result,
+                                                                    dataflow_qcap(a.ntiles));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "dataflow sweep launch", __FILE__, __LINE__);
     return PFAST_OK;
 }
 
-pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks) {
+template <int KIND>
+static pfast_status launch_dataflow_multi_k(const Sweep3Args* models, const int2* items, int nitems, int max_ntiles,
+                                            int maxiter, int* queue, int warps, int blocks, cudaStream_t st) {
+    const size_t smem = (size_t)warps * warp_smem_bytes<KIND>() + dataflow_extra_bytes(max_ntiles, true);
+    Sweep3Args unused;
+    std::memset(&unused, 0, sizeof(unused));
+    sweep3d_dataflow<KIND, true><<<blocks, warps * 32, smem, st>>>(unused, models, items, nitems, maxiter, queue,
+                                                                   nullptr, dataflow_qcap(max_ntiles));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "dataflow sweep launch", __FILE__, __LINE__);
+    return PFAST_OK;
+}
+
+pfast_status launch_sweep3_dataflow_multi(int kind, const Sweep3Args* models, const int2* items, int nitems,
+                                          int max_ntiles, int maxiter, int* queue, int warps, int blocks,
+                                          cudaStream_t st) {
+    if (nitems <= 0 || maxiter <= 0) return PFAST_OK;
+    if (warps < 1 || warps > 32 || blocks < 1 || max_ntiles > kDataflowMaxTiles) {
+        set_last_error("dataflow sweep: bad shape (%d warps, %d blocks, %d tiles)", warps, blocks, max_ntiles);
+        return PFAST_ERR_INVALID;
+    }
     switch (kind) {
-        case kFwdPlain64: return dataflow_shape_k<kFwdPlain64>(ntiles, nact, warps, blocks);
-        case kFwdFast32: return dataflow_shape_k<kFwdFast32>(ntiles, nact, warps, blocks);
-        case kFwdPolish64: return dataflow_shape_k<kFwdPolish64>(ntiles, nact, warps, blocks);
-        case kAdjPlain64: return dataflow_shape_k<kAdjPlain64>(ntiles, nact, warps, blocks);
-        case kAdjFast32: return dataflow_shape_k<kAdjFast32>(ntiles, nact, warps, blocks);
-        case kAdjPolish64: return dataflow_shape_k<kAdjPolish64>(ntiles, nact, warps, blocks);
+        case kFwdPlain64: return launch_dataflow_multi_k<kFwdPlain64>(models, items, nitems, max_ntiles, maxiter, queue, warps, blocks, st);
+        case kFwdFast32: return launch_dataflow_multi_k<kFwdFast32>(models, items, nitems, max_ntiles, maxiter, queue, warps, blocks, st);
+        case kFwdPolish64: return launch_dataflow_multi_k<kFwdPolish64>(models, items, nitems, max_ntiles, maxiter, queue, warps, blocks, st);
+        case kAdjPlain64: return launch_dataflow_multi_k<kAdjPlain64>(models, items, nitems, max_ntiles, maxiter, queue, warps, blocks, st);
+        case kAdjFast32: return launch_dataflow_multi_k<kAdjFast32>(models, items, nitems, max_ntiles, maxiter, queue, warps, blocks, st);
+        case kAdjPolish64: return launch_dataflow_multi_k<kAdjPolish64>(models, items, nitems, max_ntiles, maxiter, queue, warps, blocks, st);
+    }
+    set_last_error("unknown sweep kind %d", kind);
+    return PFAST_ERR_INVALID;
+}
+
+pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks, bool multi) {
+    switch (kind) {
+        case kFwdPlain64: return dataflow_shape_k<kFwdPlain64>(ntiles, nact, multi, warps, blocks);
+        case kFwdFast32: return dataflow_shape_k<kFwdFast32>(ntiles, nact, multi, warps, blocks);
+        case kFwdPolish64: return dataflow_shape_k<kFwdPolish64>(ntiles, nact, multi, warps, blocks);
+        case kAdjPlain64: return dataflow_shape_k<kAdjPlain64>(ntiles, nact, multi, warps, blocks);
+        case kAdjFast32: return dataflow_shape_k<kAdjFast32>(ntiles, nact, multi, warps, blocks);
+        case kAdjPolish64: return dataflow_shape_k<kAdjPolish64>(ntiles, nact, multi, warps, blocks);
     }
     set_last_error("unknown sweep kind %d", kind);
     return PFAST_ERR_INVALID;
