@@ -219,7 +219,7 @@ def serving():
     plain = serve_bench.sweep([1.0, 2.0, 4.0], 6.0, pg.PFAST_PLAIN_FP64, pool=pool)
     res = {"mixed": mixed, "plain": plain,
            "knee_rate": {"mixed": serve_bench.knee(mixed), "plain": serve_bench.knee(plain),
-                         "rule": "first offered rate with p99 above twice the lowest rate's p99, or under 90% completed"},
+                         "rule": "first offered rate with p99 above three times the lowest rate's p99, or under 90% completed"},
            "workload": "Poisson arrivals, 70% forward / 30% gradient, 2D 201x201..1001x401 (1 reflector) and 3D "
                        "64^3..256x256x128 grids log-uniform, 1-64 sources, 50% resident-model reuse, 8 slots, "
                        "150 GB budget; latency from arrival to host result"}

@@ -181,7 +181,7 @@ def summarize(records, wall_s, rate):
             "arrival_lag_ms_p99": float(np.percentile([r["lag_ms"] for r in records], 99)) if records else 0.0}
 
 
-def knee(results, factor=2.0):
+def knee(results, factor=3.0):
     """The lowest offered rate at which p99 latency exceeds `factor` times the p99 at the lowest
     rate, or the completed requests fall below 90% of the offered rate (None: not reached)."""
     if not results:
