@@ -218,8 +218,10 @@ def serving():
     mixed = serve_bench.sweep([4.0, 16.0, 32.0, 64.0, 128.0], 6.0, pg.PFAST_MIXED, pool=pool)
     plain = serve_bench.sweep([1.0, 2.0, 4.0], 6.0, pg.PFAST_PLAIN_FP64, pool=pool)
     res = {"mixed": mixed, "plain": plain,
+           "saturation_requests_per_s": {"mixed": max(r["requests_per_s"] for r in mixed),
+                                         "plain": max(r["requests_per_s"] for r in plain)},
            "knee_rate": {"mixed": serve_bench.knee(mixed), "plain": serve_bench.knee(plain),
-                         "rule": "first offered rate with p99 above three times the lowest rate's p99, or under 90% completed"},
+                         "rule": "first offered rate with p99 above three times the lowest rate's p99, or completions under 90% of the arrivals' rate"},
            "workload": "Poisson arrivals, 70% forward / 30% gradient, 2D 201x201..1001x401 (1 reflector) and 3D "
                        "64^3..256x256x128 grids log-uniform, 1-64 sources, 50% resident-model reuse, 8 slots, "
                        "150 GB budget; latency from arrival to host result"}

@@ -170,7 +170,7 @@ def run_stream(srv, pool3, pool2, rate, duration, precision, rng, max_inflight=2
     return records, t_end - t0
 
 
-def summarize(records, wall_s, rate):
+def summarize(records, wall_s, rate, duration):
     ok = [r for r in records if r["ok"]]
     lat = np.array([r["latency_ms"] for r in ok]) if ok else np.zeros(1)
     solves = sum(r["nsrc"] * (2 if r["kind"] == "grad" else 1) for r in ok)
@@ -178,17 +178,19 @@ def summarize(records, wall_s, rate):
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_queue_ms": float(np.mean([r["queue_ms"] for r in ok])) if ok else 0.0,
             "requests_per_s": len(ok) / wall_s, "solves_per_s": solves / wall_s, "wall_s": wall_s,
-            "arrival_lag_ms_p99": float(np.percentile([r["lag_ms"] for r in records], 99)) if records else 0.0}
+            "arrival_lag_ms_p99": float(np.percentile([r["lag_ms"] for r in records], 99)) if records else 0.0,
+            "arrival_rate": len(records) / duration}
 
 
 def knee(results, factor=3.0):
     """The lowest offered rate at which p99 latency exceeds `factor` times the p99 at the lowest
-    rate, or the completed requests fall below 90% of the offered rate (None: not reached)."""
+    rate, or the completion rate falls below 90% of the stream's actual arrival rate (None: not
+    reached)."""
     if not results:
         return None
     base = results[0]["p99_ms"]
     for r in results:
-        if r["p99_ms"] > factor * base or r["requests_per_s"] < 0.9 * r["offered_rate"]:
+        if r["p99_ms"] > factor * base or r["requests_per_s"] < 0.9 * r["arrival_rate"]:
             return r["offered_rate"]
     return None
 
@@ -203,7 +205,7 @@ def sweep(rates, duration, precision, slots=8, budget_gb=150.0, seed=5, pool=Non
         recs, wall = run_stream(srv, pool3, pool2, rate, duration, precision, np.random.default_rng(seed + int(rate)))
         st = srv.stats()
         srv.close()
-        s = summarize(recs, wall, rate)
+        s = summarize(recs, wall, rate, duration)
         s["peak_gb"] = st["peak_bytes"] / 1e9
         out.append(s)
     return out
