@@ -262,8 +262,8 @@ def main():
     d_vp = torch.from_numpy(v0).cuda()
     grad = torch.empty_like(d_vp)
 
-    # ---- the FP64 roof (a DGEMM, before anything is timed), schedule autotuning on this
-    # workload (both schedules once, same bits), then warm-up
+    # ---- the FP64 roof (a DGEMM, before anything is timed), autotuning on this workload (each
+    # (schedule, tile shape) candidate once), then warm-up
     fp64_gflops = fp64_peak_gflops() if rank == 0 else None
     tune = sv.autotune(d_vp, precision=pg.PFAST_MIXED)
     # ---- device-resident timing (inputs already in HBM)
@@ -331,35 +331,42 @@ def main():
     d2h = v0.nbytes + 8
 
     # ---- roofline of the dominant kernel (the sweep kernel of the longest phase)
-    phases = {"fwd32": (st["ms_fwd32"], st["fwd_node_updates"] - st["fwd64_node_updates"], 4, "sweep3d_kernel<kFwdFast32>"),
-              "fwd64": (st["ms_fwd64"], st["fwd64_node_updates"], 8, "sweep3d_kernel<kFwdPolish64>"),
-              "adj32": (st["ms_adj32"], st["adj_node_updates"] - st["adj64_node_updates"], 4, "sweep3d_kernel<kAdjFast32>"),
-              "adj64": (st["ms_adj64"], st["adj64_node_updates"], 8, "sweep3d_kernel<kAdjPolish64>")}
+    phases = {"fwd32": (st["ms_fwd32"], st["fwd_node_updates"] - st["fwd64_node_updates"], 4, "kFwdFast32", "fwd32"),
+              "fwd64": (st["ms_fwd64"], st["fwd64_node_updates"], 8, "kFwdPolish64", "fwd64_polish"),
+              "adj32": (st["ms_adj32"], st["adj_node_updates"] - st["adj64_node_updates"], 4, "kAdjFast32", "adj32"),
+              "adj64": (st["ms_adj64"], st["adj64_node_updates"], 8, "kAdjPolish64", "adj64_polish")}
     dom = max(phases, key=lambda k: phases[k][0])
-    ms_dom, upd_dom, w, kname = phases[dom]
+    ms_dom, upd_dom, w, kind_name, kind_key = phases[dom]
+    # the (schedule, tile shape) the autotuner gave that phase
+    cand = pg._capi.phase_candidates(st).get(kind_key, "diagonal 4x8x32")
+    sched, tshape = cand.split()
     # FP64 instructions per executed node update of the polish kernels (the residual-form
     # updates; everything else in them runs on the integer and FP32 pipes)
     fp64_per_update = {"fwd32": 0, "fwd64": 7, "adj32": 0, "adj64": 13}[dom]   # isotropic grid
     alg_bytes = upd_dom * 3 * w                       # read U + read slowness/T + write U per node update
-    # launches of that kernel per evaluation: outer iterations x 8 sweep orders x tile diagonals
-    # (4 x 8 x 32 tiles: nbk + nbi + nbj - 2 diagonals)
-    ndiag = -(-NZ // 4) + -(-NR // 8) + -(-NC // 32) - 2
     iters_dom = {"fwd32": st["fwd32_iters_max"], "fwd64": st["fwd_iters_max"], "adj32": st["adj32_iters_max"],
                  "adj64": st["adj_iters_max"]}[dom]
-    launches_dom = iters_dom * 8 * ndiag
+    if sched == "persistent":   # one dataflow launch per phase and batch
+        kname = f"sweep3d_dataflow<{kind_name}, {tshape}>"
+        launches_dom = st["batches"]
+    else:   # outer iterations x 8 sweep orders x tile diagonals (nbk + nbi + nbj - 2)
+        kname = f"sweep3d_kernel<{kind_name}, {tshape}>"
+        tk, ti, tj = (int(x) for x in tshape.split("x"))
+        ndiag = -(-NZ // tk) + -(-NR // ti) + -(-NC // tj) - 2
+        launches_dom = iters_dom * 8 * ndiag * st["batches"]
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (ms_dom / 1e3) / 1e9 if ms_dom > 0 else 0.0
     # DRAM traffic per launch of the polish kernels: the algorithmic bytes per launch times the
     # ratio of measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum, 9-source
-    # case of this grid) to the algorithmic bytes of the same launches: forward polish over the
-    # 1680 per-diagonal launches of the phase; adjoint polish in the dataflow kernel, which the
-    # autotuner picks for that phase on this workload (one launch per phase).  The excess over 1
-    # is the halo re-read.
-    traffic_ratio = {"fwd64": 1.09, "adj64": 0.99}
-    traffic = (alg_bytes / launches_dom * traffic_ratio[dom]) if (dom in traffic_ratio and launches_dom) else None
+    # case of this grid) to the algorithmic bytes of the same launches, per (phase, schedule and
+    # tile shape): forward polish over the 1680 per-diagonal launches of the phase; adjoint
+    # polish in the dataflow kernel (one launch per phase).  The excess over 1 is the halo re-read.
+    traffic_ratios = {("fwd64", "diagonal 4x8x32"): 1.09, ("adj64", "persistent 4x8x32"): 0.99}
+    ratio = traffic_ratios.get((dom, cand))
+    traffic = alg_bytes / launches_dom * ratio if (ratio and launches_dom) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_unit": "bytes per launch",
-                "traffic_over_algorithmic": traffic_ratio.get(dom),
+                "traffic_over_algorithmic": ratio, "schedule": cand,
                 "algorithmic_bytes_per_launch": alg_bytes / launches_dom if launches_dom else None,
                 "kernel": kname, "phase": dom,
                 "peak_kind": peak_kind, "node_updates_per_s": upd_dom / (ms_dom / 1e3) if ms_dom > 0 else 0.0,
@@ -403,6 +410,7 @@ def main():
                 "autotune_ms": {k: v["ms_total"] for k, v in tune.items()},
                 "step_ms": step_ms,
                 "phase_ms": {k: st[k] for k in ("ms_fwd32", "ms_fwd64", "ms_adj32", "ms_adj64", "ms_other", "ms_total")},
+                "phase_schedule": pg._capi.phase_candidates(st),
                 "iters": {k: st[k] for k in ("fwd32_iters_max", "fwd_iters_max", "adj32_iters_max", "adj_iters_max")}}
     sv.close()
     ctx.close()

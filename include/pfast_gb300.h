@@ -50,22 +50,32 @@ typedef struct {
                              (adjoint: times 1 + |lambda|) are dropped, so converged regions reach
                              a bitwise fixed point; 0 = the default, 1e-10.  Keep it well below the
                              1e-9 convergence tolerance. */
-    int schedule;         /* 3D sweeps: 0 = automatic (per sweep kind, the faster one measured by
-                             pfast_survey3d_autotune for this grid shape and source count; untuned:
-                             persistent from 2 sources per SM), 1 = one launch per tile diagonal
-                             (every tile of every source spread over all SMs), 2 = persistent: one
-                             dataflow launch per phase, one block solves one source with its sweep
-                             orders overlapping as the tile dependencies allow (grids of at most
-                             8192 tiles of 4x8x32 nodes; larger grids use 1).  Same results. */
+    int schedule;         /* 3D sweeps: 0 = automatic (per sweep kind, the fastest schedule and
+                             tile shape measured by pfast_survey3d_autotune for this grid shape and
+                             source count; untuned: persistent from 2 sources per SM), 1 = one launch
+                             per tile diagonal (every tile of every source spread over all SMs), 2 =
+                             persistent: one dataflow launch per phase, one block solves one source
+                             with its sweep orders overlapping as the tile dependencies allow (grids
+                             of at most 8192 tiles; larger grids use 1).  Same results. */
     int near_source_radius;  /* 3D forward, opt-in (not in the reference): nodes within this many grid
                              nodes of the source (Euclidean, in nodes) start from the straight-ray
                              traveltime 0.5*(s_src + s_node)*distance and stay fixed, which removes most
                              of the first-order scheme's source error.  0 = off (the reference's
                              point-source start; results bit-identical to it). */
+    int tile_shape;       /* 3D sweeps: nodes per tile (one warp updates one tile), in sweep-order
+                             axes (z, rows, columns): 0 = automatic (as schedule 0; untuned 4x8x32),
+                             1 = 4x8x32, 2 = 8x4x32.  Plain FP64 results are bit-identical for both
+                             shapes; in the mixed mode the FP64 polish may stop at other bits within
+                             its 1e-9 tolerance. */
 } pfast_options;
 #define PFAST_SCHEDULE_AUTO 0
 #define PFAST_SCHEDULE_DIAGONAL 1
 #define PFAST_SCHEDULE_PERSISTENT 2
+#define PFAST_TILE_AUTO 0
+#define PFAST_TILE_4x8x32 1
+#define PFAST_TILE_8x4x32 2
+/* Candidates of the autotuner: (schedule, tile shape) pairs, index = 2*(schedule-1) + (shape-1). */
+#define PFAST_TUNE_CANDIDATES 4
 
 typedef struct {
     long long fwd_node_updates;   /* executed node updates, forward sweeps (all precisions) */
@@ -83,6 +93,10 @@ typedef struct {
     double ms_adj32, ms_adj64;
     double ms_other;              /* initialisation, receiver conditions, gradient sums */
     double ms_total;
+    int candidates;               /* 3D: per sweep kind k -- 0 plain forward, 1 FP32 forward, 2 polish
+                                     forward, 3 plain adjoint, 4 FP32 adjoint, 5 polish adjoint -- bits
+                                     4k..4k+3: 1 + the (schedule, tile shape) candidate (index as in
+                                     pfast_survey3d_autotune) of its last phase; 0 = kind not run */
 } pfast_stats;
 
 /* ------------------------------------------------------------------ library */
@@ -145,12 +159,15 @@ pfast_status pfast_survey3d_eval(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
 pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp,
                                     const pfast_options* opt, double* picks, pfast_stats* stats);
 
-/* Schedule autotuner: runs the survey's evaluation (gradient when it has picks, else picks)
- * once per sweep schedule on the DEVICE model vp and records each phase's time per (sweep
- * kind, grid shape, source count); later automatic-schedule calls of the same shape use the
- * faster schedule.  Both schedules give identical results.  stats_*: optional. */
+/* Schedule and tile-shape autotuner: runs the survey's evaluation (gradient when it has picks,
+ * else picks) once per candidate (schedule, tile shape) -- per-diagonal 4x8x32, per-diagonal
+ * 8x4x32, persistent 4x8x32, persistent 8x4x32 -- on the DEVICE model vp and records each
+ * phase's time per (sweep kind, grid shape, source count); later calls with schedule and
+ * tile_shape both automatic use, per phase, the fastest candidate.  stats: null, or an array of
+ * PFAST_TUNE_CANDIDATES records in that order (a persistent candidate whose grid does not fit
+ * the dataflow kernel runs per diagonal). */
 pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
-                                     pfast_stats* stats_diagonal, pfast_stats* stats_persistent);
+                                     pfast_stats* stats);
 
 /* Misfit + gradient of n independent (model, survey) pairs at once: the reference's per-model
  * evaluation (the source loop of src/T_PFAST3D.cpp:387-399, one model per run) for many models

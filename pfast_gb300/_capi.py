@@ -22,11 +22,14 @@ PFAST_ERR_LINE_SEARCH = 8
 PFAST_PLAIN_FP64 = 0
 PFAST_MIXED = 1
 PFAST_SCHEDULE_AUTO, PFAST_SCHEDULE_DIAGONAL, PFAST_SCHEDULE_PERSISTENT = 0, 1, 2
+PFAST_TILE_AUTO, PFAST_TILE_4x8x32, PFAST_TILE_8x4x32 = 0, 1, 2
+# autotuner candidates, in the order of pfast_survey3d_autotune's stats array
+PFAST_TUNE_CANDIDATES = ("diagonal 4x8x32", "diagonal 8x4x32", "persistent 4x8x32", "persistent 8x4x32")
 
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("maxswp", C.c_int), ("max_batch", C.c_int), ("polish_floor", C.c_double),
-                ("schedule", C.c_int), ("near_source_radius", C.c_int)]
+                ("schedule", C.c_int), ("near_source_radius", C.c_int), ("tile_shape", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -39,11 +42,21 @@ class Stats(C.Structure):
         ("launches", C.c_longlong),
         ("ms_fwd32", C.c_double), ("ms_fwd64", C.c_double),
         ("ms_adj32", C.c_double), ("ms_adj64", C.c_double),
-        ("ms_other", C.c_double), ("ms_total", C.c_double),
+        ("ms_other", C.c_double), ("ms_total", C.c_double), ("candidates", C.c_int),
     ]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+SWEEP_KINDS = ("fwd64_plain", "fwd32", "fwd64_polish", "adj64_plain", "adj32", "adj64_polish")
+
+
+def phase_candidates(stats):
+    """{sweep kind: (schedule, tile shape) candidate name} of the phases an evaluation ran,
+    decoded from pfast_stats.candidates."""
+    c = int(stats["candidates"])
+    return {k: PFAST_TUNE_CANDIDATES[(c >> 4 * i & 15) - 1] for i, k in enumerate(SWEEP_KINDS) if c >> 4 * i & 15}
 
 
 PFAST_SCHEME_HS, PFAST_SCHEME_CGDESCENT, PFAST_SCHEME_LBFGS = 1, 2, 3
@@ -99,6 +112,16 @@ class RequestResult(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+SWEEP_KINDS = ("fwd64_plain", "fwd32", "fwd64_polish", "adj64_plain", "adj32", "adj64_polish")
+
+
+def phase_candidates(stats):
+    """{sweep kind: (schedule, tile shape) candidate name} of the phases an evaluation ran,
+    decoded from pfast_stats.candidates."""
+    c = int(stats["candidates"])
+    return {k: PFAST_TUNE_CANDIDATES[(c >> 4 * i & 15) - 1] for i, k in enumerate(SWEEP_KINDS) if c >> 4 * i & 15}
+
+
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
                 ("running", C.c_int), ("waiting", C.c_int), ("resident_models", C.c_int),
@@ -107,6 +130,16 @@ class ServerStats(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+SWEEP_KINDS = ("fwd64_plain", "fwd32", "fwd64_polish", "adj64_plain", "adj32", "adj64_polish")
+
+
+def phase_candidates(stats):
+    """{sweep kind: (schedule, tile shape) candidate name} of the phases an evaluation ran,
+    decoded from pfast_stats.candidates."""
+    c = int(stats["candidates"])
+    return {k: PFAST_TUNE_CANDIDATES[(c >> 4 * i & 15) - 1] for i, k in enumerate(SWEEP_KINDS) if c >> 4 * i & 15}
 
 
 # (name, restype, argtypes) of every entry point in include/pfast_gb300.h
@@ -130,7 +163,7 @@ SIGNATURES = [
     ("pfast_survey3d_destroy", _i, [_p]),
     ("pfast_survey3d_eval", _i, [_p, _p, _p, _p, _p, _p, _p]),
     ("pfast_survey3d_forward", _i, [_p, _p, _p, _p, _p, _p]),
-    ("pfast_survey3d_autotune", _i, [_p, _p, _p, _p, _p, _p]),
+    ("pfast_survey3d_autotune", _i, [_p, _p, _p, _p, _p]),
     ("pfast_surveys3d_eval", _i, [_p, _i, _p, _p, _p, _p, _p, _p]),
     ("pfast_eval3d", _i, [_p, _p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     ("pfast_forward3d", _i, [_p, _p, _i, _i, _i, _d, _d, _d, _i, _p, _p, _p, _p, _p, _p]),

@@ -88,7 +88,7 @@ def Radjoint_fsm2d(UR, Td, Tu, TR_obs, rec, nxyz, src, srnum, srcid, NumofR, MAX
 
 
 # ------------------------------------------------------------ batched layer
-def _opts(precision, maxswp, max_batch, polish_floor=0.0, schedule=0, near_source_radius=0):
+def _opts(precision, maxswp, max_batch, polish_floor=0.0, schedule=0, near_source_radius=0, tile_shape=0):
     o = _capi.Options()
     o.precision = int(precision)
     o.maxswp = int(maxswp)
@@ -96,6 +96,7 @@ def _opts(precision, maxswp, max_batch, polish_floor=0.0, schedule=0, near_sourc
     o.polish_floor = float(polish_floor)
     o.schedule = int(schedule)
     o.near_source_radius = int(near_source_radius)
+    o.tile_shape = int(tile_shape)
     return o
 
 
@@ -173,39 +174,41 @@ class Survey3D:
               "survey3d_create")
 
     def eval(self, vp, grad=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0, polish_floor=0.0, schedule=0,
-             near_source_radius=0):
+             near_source_radius=0, tile_shape=0):
         """Misfit + gradient for the device model vp (torch float64 [nz, nrows, ncols]).
-        Returns (grad tensor, misfit, stats dict)."""
+        schedule / tile_shape: 0 automatic, else as pfast_options.  Returns (grad tensor,
+        misfit, stats dict)."""
         import torch
         n = int(np.prod(self.shape))
         if grad is None:
             grad = torch.empty(self.shape, dtype=torch.float64, device=vp.device)
         E = C.c_double(0)
         st = _capi.Stats()
-        o = _opts(precision, maxswp, max_batch, polish_floor, schedule, near_source_radius)
+        o = _opts(precision, maxswp, max_batch, polish_floor, schedule, near_source_radius, tile_shape)
         check(lib().pfast_survey3d_eval(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
                                         _dev_ptr(grad, "grad", numel=n), C.addressof(E), C.byref(st)), "survey3d_eval")
         return grad, E.value, st.as_dict()
 
     def autotune(self, vp, precision=PFAST_MIXED, maxswp=100):
-        """Time both sweep schedules on this survey and model (pfast_survey3d_autotune); later
-        automatic-schedule evaluations of this grid and source count use the faster one.
-        Returns the per-schedule stats."""
-        sd, sp = _capi.Stats(), _capi.Stats()
+        """Time every (schedule, tile shape) candidate on this survey and model
+        (pfast_survey3d_autotune); later automatic evaluations of this grid and source count
+        use, per sweep phase, the fastest one.  Returns {candidate name: stats}."""
+        n = len(_capi.PFAST_TUNE_CANDIDATES)
+        sts = (_capi.Stats * n)()
         o = _opts(precision, maxswp, 0)
         check(lib().pfast_survey3d_autotune(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=int(np.prod(self.shape))),
-                                            C.byref(o), C.byref(sd), C.byref(sp)), "survey3d_autotune")
-        return {"diagonal": sd.as_dict(), "persistent": sp.as_dict()}
+                                            C.byref(o), sts), "survey3d_autotune")
+        return {name: sts[c].as_dict() for c, name in enumerate(_capi.PFAST_TUNE_CANDIDATES)}
 
     def forward(self, vp, picks=None, precision=PFAST_PLAIN_FP64, maxswp=100, max_batch=0, polish_floor=0.0,
-                schedule=0, near_source_radius=0):
+                schedule=0, near_source_radius=0, tile_shape=0):
         """First-arrival picks [sum(srnum)] for the device model vp.  Returns (picks, stats)."""
         import torch
         n = int(np.prod(self.shape))
         if picks is None:
             picks = torch.empty(max(self.nrec, 1), dtype=torch.float64, device=vp.device)
         st = _capi.Stats()
-        o = _opts(precision, maxswp, max_batch, polish_floor, schedule, near_source_radius)
+        o = _opts(precision, maxswp, max_batch, polish_floor, schedule, near_source_radius, tile_shape)
         check(lib().pfast_survey3d_forward(self.ctx.handle, self._h, _dev_ptr(vp, "vp", numel=n), C.byref(o),
                                            _dev_ptr(picks, "picks", numel=self.nrec), C.byref(st)), "survey3d_forward")
         return picks[:self.nrec], st.as_dict()

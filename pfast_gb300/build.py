@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libpfast_gb300.so")
-SOURCES = ["kernels3d.cu", "kernels2d.cu", "engine.cu", "engine2d.cu", "multi3d.cu", "noalloc.cu", "invert.cu", "serve.cu"]
+SOURCES = ["kernels3d.cu", "kernels3d_s84.cu", "kernels2d.cu", "engine.cu", "engine2d.cu", "multi3d.cu", "noalloc.cu", "invert.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"] + ARCH

@@ -32,6 +32,34 @@ static_assert(PS >= HI * HJ && (PS - 1) % 32 == 8 && (HJ - 1) % 32 == 1, "bank-c
 // Interior tile (the forward's staged slowness) layout, flipped like the box: [TK][SPS] with rows of SJ.
 constexpr int SJ = TJ + 2, SPS = 297;
 static_assert(SPS >= TI * SJ && (SPS - 1) % 32 == 8, "bank-conflict-free stride");
+// Tile shapes.  One warp sweeps a TK x TI x TJ tile, lane = (kf, if) with TK*TI = 32, TJ = 32;
+// the halo box's plane stride PS is the smallest >= HI*HJ with PS - 1 = TI (mod 32), so that the
+// lanes of a wavefront step, at kf*(PS-1) + if*(HJ-1) + t, hit 32 distinct banks; the staged
+// interior tile's plane stride SPS likewise.  Shape 0 is 4x8x32 (the constants above), shape 1
+// 8x4x32: the same 1024 nodes and 42 wavefront steps, half as many tiles along z and twice as
+// many along the rows.
+template <int TK_, int TI_>
+struct TileShape {
+    static constexpr int TK = TK_, TI = TI_, TJ = 32;
+    static constexpr int HK = TK + 2, HI = TI + 2, HJ = TJ + 2;
+    static constexpr int PS = HI * HJ + ((TI + 1 - HI * HJ) % 32 + 32) % 32;
+    static constexpr int SJ = TJ + 2;
+    static constexpr int SPS = TI * SJ + ((TI + 1 - TI * SJ) % 32 + 32) % 32;
+    static_assert(TK * TI == 32 && (PS - 1) % 32 == TI && (HJ - 1) % 32 == 1 && (SPS - 1) % 32 == TI,
+                  "bank-conflict-free strides");
+};
+using Shape48 = TileShape<4, 8>;
+using Shape84 = TileShape<8, 4>;
+static_assert(Shape48::PS == PS && Shape48::SPS == SPS && Shape48::TK == TK && Shape48::TI == TI, "shape 0");
+constexpr int kTileShapes = 2;
+__host__ __device__ constexpr int shape_tk(int shape) { return shape ? Shape84::TK : Shape48::TK; }
+__host__ __device__ constexpr int shape_ti(int shape) { return shape ? Shape84::TI : Shape48::TI; }
+// Inside code templated on a shape SH: its constants under the usual names.
+#define PFAST_TILE_SHAPE(SH)                                                                          \
+    constexpr int TK = SH::TK, TI = SH::TI, TJ = SH::TJ, HK = SH::HK, HI = SH::HI, HJ = SH::HJ;       \
+    constexpr int PS = SH::PS, SJ = SH::SJ, SPS = SH::SPS;                                           \
+    (void)TK; (void)TI; (void)TJ; (void)HK; (void)HI; (void)HJ; (void)PS; (void)SJ; (void)SPS
+
 // Warps (tiles) per CTA.
 constexpr int kDataflowMaxTiles = 8192;   // tiles per instance the dataflow kernel keeps in shared memory
 constexpr int kWarps3 = 1;   // one-warp CTAs: the finest shared-memory granularity, hence the most warps per SM

@@ -104,12 +104,12 @@ void add_elapsed(cudaEvent_t a, cudaEvent_t b, double* acc) {
     if (cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && acc) *acc += ms;
 }
 
-pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, DiagTable3** out) {
-    auto key = std::make_tuple(nz, nr, nc);
+pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, int shape, DiagTable3** out) {
+    auto key = std::make_tuple(nz, nr, nc, shape);
     auto it = ctx->diag3.find(key);
     if (it == ctx->diag3.end()) {
         DiagTable3 t;
-        PFAST_TRY(build_diag_table3(nz, nr, nc, t));
+        PFAST_TRY(build_diag_table3(nz, nr, nc, shape, t));
         it = ctx->diag3.emplace(key, t).first;
     }
     *out = &it->second;
@@ -156,24 +156,38 @@ Spacing3 make_spacing(double dx, double dy, double dz) {
 
 // Run outer iterations of `kind` over the active batch instances until each one
 // converges or reaches maxiter.  iters[b] receives the iteration count of instance b.
-// Schedule autotuner, per (device, sweep kind, grid, active instances): phase times of the two
-// schedules measured by pfast_survey3d_autotune, which runs the same evaluation once with each
-// (identical inputs, identical bits).  An automatic phase uses the faster one once both are
-// known; before that, the dataflow kernel from two instances per SM, else one launch per tile
-// diagonal.
+// Autotuner, per (device, sweep kind, grid, active instances): phase times of the candidate
+// (schedule, tile shape) pairs -- c = 2*persistent + shape -- measured by pfast_survey3d_autotune,
+// which runs the same evaluation once with each.  A phase picks, among the candidates its options
+// allow and its grid fits, the fastest one once all of them are measured; before that, the
+// dataflow kernel from two instances per SM (else one launch per tile diagonal) with 4x8x32 tiles.
 struct TuneEntry {
-    double ms[2] = {0.0, 0.0};
-    int n[2] = {0, 0};
+    double ms[4] = {0.0, 0.0, 0.0, 0.0};
+    int n[4] = {0, 0, 0, 0};
 };
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int, int, int>, TuneEntry> g_tune;
 
-static int tuned_schedule(const std::tuple<int, int, int, int, int, int>& key, int sms) {
+static int tuned_candidate(const std::tuple<int, int, int, int, int, int>& key, unsigned allowed, int sms) {
     std::lock_guard<std::mutex> g(g_tune_mu);
     auto it = g_tune.find(key);
-    if (it != g_tune.end() && it->second.n[0] > 0 && it->second.n[1] > 0)
-        return it->second.ms[1] / it->second.n[1] < it->second.ms[0] / it->second.n[0] ? 1 : 0;
-    return std::get<5>(key) >= 2 * sms ? 1 : 0;
+    if (it != g_tune.end()) {
+        int best = -1;
+        bool all = true;
+        for (int c = 0; c < 4; ++c) {
+            if (!(allowed >> c & 1)) continue;
+            if (it->second.n[c] == 0) { all = false; break; }
+            const double t = it->second.ms[c] / it->second.n[c];
+            if (best < 0 || t < it->second.ms[best] / it->second.n[best]) best = c;
+        }
+        if (all && best >= 0) return best;
+    }
+    const int first = std::get<5>(key) >= 2 * sms && (allowed & 0xc) ? 2 : 0;
+    for (int c = first; c < 4; ++c)
+        if (allowed >> c & 1) return c;
+    for (int c = 0; c < 4; ++c)
+        if (allowed >> c & 1) return c;
+    return 0;
 }
 
 static void tune_record(const std::tuple<int, int, int, int, int, int>& key, int which, double ms) {
@@ -250,9 +264,40 @@ int rows_aligned_impl(const Sweep3Args& a, int kind) {
     return 1;
 }
 
-pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable3& dt, int nb,
-                         std::vector<int>& active, int maxiter, int* iters, long long nodes_per_sweep,
-                         long long* node_updates, int* not_conv, double* ms_acc) {
+pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::vector<int>& active, int maxiter,
+                         int* iters, long long nodes_per_sweep, long long* node_updates, int* not_conv,
+                         double* ms_acc) {
+    // Two schedules.  Per-diagonal launches spread every tile of every active instance over
+    // all SMs (one warp per tile) and suit surveys with few instances; the dataflow kernel
+    // (one block solves one instance, its sweep orders overlapping as their tile dependencies
+    // allow, no host round trip per iteration) suits runs with about one instance per SM or
+    // more.  Two tile shapes, 4x8x32 and 8x4x32 nodes in sweep-order axes.  Automatic: the
+    // autotuner above.  Grids whose tiles do not fit the dataflow kernel's shared memory use
+    // the per-diagonal launches.
+    int dev = 0, sms = 1;
+    PFAST_CUDA_TRY(cudaGetDevice(&dev));
+    PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const auto tkey = std::make_tuple(dev, kind, a.nz, a.nr, a.nc, (int)active.size());
+    int dwarps[kTileShapes] = {}, dblocks[kTileShapes] = {};
+    unsigned allowed = 0;
+    for (int shape = 0; shape < kTileShapes; ++shape) {
+        if (ctx->tile_shape != PFAST_TILE_AUTO && ctx->tile_shape - 1 != shape) continue;
+        DiagTable3* t = nullptr;
+        PFAST_TRY(ctx_diag3(ctx, a.nz, a.nr, a.nc, shape, &t));
+        const int ntl = t->nbk * t->nbi * t->nbj;
+        if (!active.empty()) PFAST_TRY(dataflow_shape(kind, shape, ntl, (int)active.size(), &dwarps[shape], &dblocks[shape]));
+        if (ctx->schedule != PFAST_SCHEDULE_PERSISTENT) allowed |= 1u << shape;
+        if (ctx->schedule != PFAST_SCHEDULE_DIAGONAL && dwarps[shape] > 0) allowed |= 4u << shape;
+    }
+    if (!allowed)   // persistent asked for, but the grid does not fit the dataflow kernel
+        allowed = ctx->tile_shape == PFAST_TILE_AUTO ? 1u : 1u << (ctx->tile_shape - 1);
+    const int cand = tuned_candidate(tkey, allowed, sms);
+    ctx->candidates = (ctx->candidates & ~(15 << 4 * kind)) | (cand + 1) << 4 * kind;
+    const bool persistent = cand >= 2;
+    a.shape = cand & 1;
+    DiagTable3* dtp = nullptr;
+    PFAST_TRY(ctx_diag3(ctx, a.nz, a.nr, a.nc, a.shape, &dtp));
+    const DiagTable3& dt = *dtp;
     a.vec_rows = rows_aligned_impl(a, kind);
     PFAST_TRY(ctx->act.ensure(sizeof(int) * nb));
     PFAST_TRY(ctx->changed.ensure(sizeof(int) * nb));
@@ -293,28 +338,14 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
         // initial selected orders per tile, so the first polish sweep skips unselected tiles
         if (polish) PFAST_LAUNCH(ctx, launch_polish_orders3(kind, a, nb, nact0, st));
     }
-    // Two schedules.  Per-diagonal launches spread every tile of every active instance over
-    // all SMs (one warp per tile) and suit surveys with few instances; the dataflow kernel
-    // (one block solves one instance, its sweep orders overlapping as their tile dependencies
-    // allow, no host round trip per iteration) suits runs with about one instance per SM or
-    // more.  Automatic: the autotuner above.  Grids whose tiles do not fit the dataflow
-    // kernel's shared memory use the per-diagonal launches.
-    int dev = 0, sms = 1;
-    PFAST_CUDA_TRY(cudaGetDevice(&dev));
-    PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const auto tkey = std::make_tuple(dev, kind, a.nz, a.nr, a.nc, (int)active.size());
-    int dwarps = 0, dblocks = 0;
-    if (!active.empty()) PFAST_TRY(dataflow_shape(kind, a.ntiles, (int)active.size(), &dwarps, &dblocks));
-    const bool persistent = dwarps > 0 &&
-                            (ctx->schedule == PFAST_SCHEDULE_PERSISTENT ||
-                             (ctx->schedule == PFAST_SCHEDULE_AUTO && tuned_schedule(tkey, sms) == 1));
     if (persistent && maxiter > 0) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
         PFAST_TRY(ctx->queue.ensure(2 * sizeof(int)));
         PFAST_CUDA_TRY(cudaMemsetAsync(ctx->queue.p, 0, 2 * sizeof(int), st));
-        PFAST_TRY(launch_sweep3_dataflow(kind, a, nact, maxiter, ctx->queue.as<int>(), a.changed, dwarps, dblocks, st));
+        PFAST_TRY(launch_sweep3_dataflow(kind, a, nact, maxiter, ctx->queue.as<int>(), a.changed, dwarps[a.shape],
+                                         dblocks[a.shape], st));
         ++ctx->launches;
         PFAST_TRY(ctx->h_dyn.ensure(2 * sizeof(int)));
         int* hq = ctx->h_dyn.as<int>();
@@ -395,7 +426,7 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, const DiagTable
     double ms = 0.0;
     add_elapsed(ctx->ev[0], ctx->ev[1], &ms);
     if (ms_acc) *ms_acc += ms;
-    if (ctx->tuning) tune_record(tkey, persistent ? 1 : 0, ms);
+    if (ctx->tuning) tune_record(tkey, cand, ms);
     return PFAST_OK;
 }
 
@@ -439,8 +470,6 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
                              pfast_stats* st) {
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
     cudaStream_t s = ctx->stream;
-    DiagTable3* dt = nullptr;
-    PFAST_TRY(ctx_diag3(ctx, sv->nz, sv->nr, sv->nc, &dt));
     PFAST_TRY(ctx->T64.ensure(sizeof(double) * N * nb));
     PFAST_TRY(ctx->scratch.ensure(sizeof(double) * N * nb));
     std::vector<int> iters(nb, 0), active(nb);
@@ -464,7 +493,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
-        PFAST_TRY(run_sweeps3(ctx, a, kFwdPlain64, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
+        PFAST_TRY(run_sweeps3(ctx, a, kFwdPlain64, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
                               st ? &st->ms_fwd64 : nullptr));
         if (st) {
             st->fwd64_node_updates += *nu - before;
@@ -482,7 +511,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.aux = ctx->s32.p;
         a.tol_abs_f = 0.0f;
         a.tol_rel_f = (float)kTol32Rel;
-        PFAST_TRY(run_sweeps3(ctx, a, kFwdFast32, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
+        PFAST_TRY(run_sweeps3(ctx, a, kFwdFast32, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
                               st ? &st->ms_fwd32 : nullptr));
         if (st) for (int v : iters) st->fwd32_iters_max = std::max(st->fwd32_iters_max, v);
         PFAST_LAUNCH(ctx, launch_widen(T32, ctx->T64.as<double>(), N, N, N, nb, s));
@@ -500,7 +529,7 @@ pfast_status forward3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
-        PFAST_TRY(run_sweeps3(ctx, a, kFwdPolish64, *dt, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
+        PFAST_TRY(run_sweeps3(ctx, a, kFwdPolish64, nb, active, maxswp, iters.data(), N, nu, nc_ptr,
                               st ? &st->ms_fwd64 : nullptr));
         if (st) {
             st->fwd64_node_updates += *nu - before;
@@ -516,8 +545,6 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
     const int wpr = (sv->nc + 31) / 32;
     const long long mwords = (long long)sv->nz * sv->nr * wpr;
     cudaStream_t s = ctx->stream;
-    DiagTable3* dt = nullptr;
-    PFAST_TRY(ctx_diag3(ctx, sv->nz, sv->nr, sv->nc, &dt));
     PFAST_TRY(ctx->L64.ensure(sizeof(double) * N * nb));
     PFAST_TRY(ctx->scratch.ensure(sizeof(double) * N * nb));
     PFAST_TRY(ctx->mask.ensure(sizeof(unsigned) * mwords * nb));
@@ -576,7 +603,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
-        PFAST_TRY(run_sweeps3(ctx, a, kAdjPlain64, *dt, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
+        PFAST_TRY(run_sweeps3(ctx, a, kAdjPlain64, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
                               st ? &st->ms_adj64 : nullptr));
         if (st) {
             st->adj64_node_updates += *nu - before;
@@ -593,7 +620,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.aux = ctx->T32.p;
         a.tol_abs_f = (float)kTol32AbsAdj;
         a.tol_rel_f = (float)kTol32Rel;
-        PFAST_TRY(run_sweeps3(ctx, a, kAdjFast32, *dt, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
+        PFAST_TRY(run_sweeps3(ctx, a, kAdjFast32, nb, active, maxswp, iters.data(), interior, nu, nc_ptr,
                               st ? &st->ms_adj32 : nullptr));
         if (st) for (int v : iters) st->adj32_iters_max = std::max(st->adj32_iters_max, v);
         PFAST_LAUNCH(ctx, launch_widen_lambda(L32, ctx->L64.as<double>(), ctx->mask.as<unsigned>(), N, N, mwords, sv->nz,
@@ -606,7 +633,7 @@ pfast_status adjoint3d_batch(pfast_ctx* ctx, const pfast_survey3d* sv, int b0, i
         a.tol_abs = kConvTol;
         a.tol_rel = 0.0;
         long long before = nu ? *nu : 0;
-        PFAST_TRY(run_sweeps3(ctx, a, kAdjPolish64, *dt, nb, active64, maxswp, iters.data(), interior, nu, nc_ptr,
+        PFAST_TRY(run_sweeps3(ctx, a, kAdjPolish64, nb, active64, maxswp, iters.data(), interior, nu, nc_ptr,
                               st ? &st->ms_adj64 : nullptr));
         if (st) {
             st->adj64_node_updates += *nu - before;
@@ -640,6 +667,10 @@ bool valid_options_impl(const pfast_options* opt) {
         set_last_error("near_source_radius must be in [0, 64]");
         return false;
     }
+    if (opt->tile_shape < PFAST_TILE_AUTO || opt->tile_shape > PFAST_TILE_8x4x32) {
+        set_last_error("unknown tile_shape %d", opt->tile_shape);
+        return false;
+    }
     return true;
 }
 
@@ -651,6 +682,7 @@ pfast_options resolve_impl(const pfast_options* opt, int default_maxswp) {
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
     o.near_source_radius = 0;
+    o.tile_shape = PFAST_TILE_AUTO;
     if (opt) o = *opt;
     return o;
 }
@@ -713,6 +745,7 @@ void pfast_default_options(pfast_options* opt) {
     opt->polish_floor = 0.0;
     opt->schedule = PFAST_SCHEDULE_AUTO;
     opt->near_source_radius = 0;
+    opt->tile_shape = PFAST_TILE_AUTO;
 }
 
 pfast_status pfast_ctx_create(int device, pfast_ctx** out) {
@@ -872,8 +905,10 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     pfast_options o = resolve_impl(opt, 100);
     ctx->polish_floor = o.polish_floor > 0.0 ? (float)o.polish_floor : kPolishFloor;
     ctx->schedule = o.schedule;
+    ctx->tile_shape = o.tile_shape;
     ctx->near_radius = o.near_source_radius;
     stats_begin_impl(stats);
+    ctx->candidates = 0;
     PFAST_CUDA_TRY(cudaSetDevice(ctx->device));
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
     cudaStream_t s = ctx->stream;
@@ -906,6 +941,7 @@ static pfast_status survey3d_run(pfast_ctx* ctx, pfast_survey3d* sv, const doubl
     if (stats) {
         add_elapsed(t0, t1, &stats->ms_total);
         stats->launches = ctx->launches - launches0;
+        stats->candidates = ctx->candidates;
     }
     if (misfit) *misfit = E;
     return PFAST_OK;
@@ -924,20 +960,21 @@ pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const do
 }
 
 pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const double* vp, const pfast_options* opt,
-                                     pfast_stats* stats_diagonal, pfast_stats* stats_persistent) {
+                                     pfast_stats* stats) {
     if (!ctx || !sv || !vp) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
     if (!valid_options_impl(opt)) return PFAST_ERR_INVALID;
     const long long N = (long long)sv->nz * sv->nr * sv->nc;
     PFAST_TRY(ctx->out_a.ensure(sizeof(double) * std::max<long long>(N, sv->nrec)));
     pfast_options o = resolve_impl(opt, 100);
-    pfast_stats* sts[2] = {stats_diagonal, stats_persistent};
     ctx->tuning = true;
     pfast_status r = PFAST_OK;
-    for (int which = 0; which < 2 && r == PFAST_OK; ++which) {
-        o.schedule = which == 0 ? PFAST_SCHEDULE_DIAGONAL : PFAST_SCHEDULE_PERSISTENT;
+    for (int c = 0; c < PFAST_TUNE_CANDIDATES && r == PFAST_OK; ++c) {
+        o.schedule = c < 2 ? PFAST_SCHEDULE_DIAGONAL : PFAST_SCHEDULE_PERSISTENT;
+        o.tile_shape = PFAST_TILE_4x8x32 + (c & 1);
+        pfast_stats* sc = stats ? stats + c : nullptr;
         double E = 0.0;
-        r = sv->has_picks ? survey3d_run(ctx, sv, vp, &o, ctx->out_a.as<double>(), &E, nullptr, sts[which])
-                          : survey3d_run(ctx, sv, vp, &o, nullptr, nullptr, ctx->out_a.as<double>(), sts[which]);
+        r = sv->has_picks ? survey3d_run(ctx, sv, vp, &o, ctx->out_a.as<double>(), &E, nullptr, sc)
+                          : survey3d_run(ctx, sv, vp, &o, nullptr, nullptr, ctx->out_a.as<double>(), sc);
     }
     ctx->tuning = false;
     return r;

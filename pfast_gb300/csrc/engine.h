@@ -63,12 +63,14 @@ struct pfast_ctx {
     // (uneven batches, a serving mix) do not pay for a graph they never replay
     std::vector<std::vector<unsigned char>> graph_seen;
     bool graphs = true;                 // replay per-diagonal outer iterations as CUDA graphs
-    std::map<std::tuple<int, int, int>, pfast::DiagTable3> diag3;
+    std::map<std::tuple<int, int, int, int>, pfast::DiagTable3> diag3;   // (nz, nr, nc, tile shape)
     std::map<std::pair<int, int>, pfast::DiagTable2> diag2;
     cudaEvent_t ev[8] = {};
     long long launches = 0;
     float polish_floor = pfast::kPolishFloor;   // of the current 3D evaluation (pfast_options)
     int schedule = PFAST_SCHEDULE_AUTO;         // of the current 3D evaluation (pfast_options)
+    int tile_shape = PFAST_TILE_AUTO;           // of the current 3D evaluation (pfast_options)
+    int candidates = 0;                         // per sweep kind: 1 + candidate of its last phase (pfast_stats)
     int near_radius = 0;                        // of the current 3D evaluation (pfast_options)
     bool tuning = false;                        // record phase times for the schedule autotuner
 };
@@ -150,7 +152,7 @@ void mark_last_rows(int r0, int r1, NodeOf node_of, Picked picked, Mark mark, st
     for (size_t h : used) keys[h] = -1;
 }
 
-pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, DiagTable3** out);
+pfast_status ctx_diag3(pfast_ctx* ctx, int nz, int nr, int nc, int shape, DiagTable3** out);
 pfast_status ctx_diag2(pfast_ctx* ctx, int nr, int nc, DiagTable2** out);
 
 // The process-wide context of the calling thread's current device (reference shims).

@@ -619,6 +619,7 @@ pfast_status forward2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
     o.near_source_radius = 0;
+    o.tile_shape = PFAST_TILE_AUTO;
     if (opt) o = *opt;
     if (o.near_source_radius < 0 || o.near_source_radius > 64) {
         set_last_error("near_source_radius must be in [0, 64]");
@@ -682,6 +683,7 @@ pfast_status eval2d_impl(pfast_ctx* ctx, pfast_survey2d* sv, const double* vp, c
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
     o.near_source_radius = 0;
+    o.tile_shape = PFAST_TILE_AUTO;
     if (opt) o = *opt;
     if (o.near_source_radius < 0 || o.near_source_radius > 64) {
         set_last_error("near_source_radius must be in [0, 64]");
@@ -941,6 +943,7 @@ pfast_status pfast_RT_fsm2d(double* vp, double* U, double* TTd, double* TTu, dou
     o.polish_floor = 0.0;
     o.schedule = PFAST_SCHEDULE_AUTO;
     o.near_source_radius = 0;
+    o.tile_shape = PFAST_TILE_AUTO;
     if (!r) r = forward2d_impl(ctx, sv, ctx->vp_tmp.as<double>(), &o, nullptr, TTd, TTu, U, nullptr);
     pfast_survey2d_destroy(sv);
     return r;

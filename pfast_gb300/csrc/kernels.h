@@ -41,6 +41,7 @@ struct Sweep3Args {
     float polish_floor;       // polish sweeps: corrections at or below this are dropped (seconds;
                               // adjoint: relative to 1 + |lambda|)
     unsigned long long* work; // per instance: nodes of the tiles processed (executed node updates); may be null
+    int shape;                // tile shape: 0 = 4x8x32, 1 = 8x4x32 (common.cuh: TileShape)
     int vec_rows;             // rows of the field (and of the FP32 adjoint's traveltime) start on 16-byte
                               // boundaries: nc a multiple of 16 / element size, 16-byte aligned fields;
                               // tiles then move in 16-byte vectors
@@ -52,16 +53,16 @@ struct Sweep3Args {
 // Tile-diagonal table for a grid: tiles (bk, bi, bj) in flipped coordinates with
 // bk+bi+bj = d, packed bk | bi<<10 | bj<<20.
 struct DiagTable3 {
+    int shape = 0;
     int nbk = 0, nbi = 0, nbj = 0, ndiag = 0;
     std::vector<int> h_off;
     int* d_off = nullptr;
     unsigned* d_tiles = nullptr;
 };
 
-pfast_status build_diag_table3(int nz, int nr, int nc, DiagTable3& t);
+pfast_status build_diag_table3(int nz, int nr, int nc, int shape, DiagTable3& t);
 void free_diag_table3(DiagTable3& t);
 
-size_t sweep3_smem_bytes(int kind);
 // changed[act[b]], b < nact: bit 0 = any diff over the tiles of instance act[b]; bit 1 = some
 // tile still due in some order (lock words `dirty`: order bits order_mask, selected orders
 // `shift` bits higher for the selective polish kinds).
@@ -89,13 +90,29 @@ pfast_status launch_sweep3_dataflow(int kind, const Sweep3Args& a, int nact, int
 // The dataflow kernel over instances of several grids: item q is instance items[q].y of the grid
 // whose arguments are models[items[q].x] (a device array; each model's result goes to its own
 // `changed` array); max_ntiles: the largest grid's tile count (<= kDataflowMaxTiles); warps and
-// blocks from dataflow_shape(kind, max_ntiles, nitems, warps, blocks, true).
-pfast_status launch_sweep3_dataflow_multi(int kind, const Sweep3Args* models, const int2* items, int nitems,
+// blocks from dataflow_shape(kind, shape, max_ntiles, nitems, warps, blocks, true).
+pfast_status launch_sweep3_dataflow_multi(int kind, int shape, const Sweep3Args* models, const int2* items, int nitems,
                                           int max_ntiles, int maxiter, int* queue, int warps, int blocks,
                                           cudaStream_t st);
 // Warps per block (as many as shared memory holds) and resident blocks
 // of the dataflow kernel; *warps = 0 when a grid of ntiles tiles does not fit.
-pfast_status dataflow_shape(int kind, int ntiles, int nact, int* warps, int* blocks, bool multi = false);
+pfast_status dataflow_shape(int kind, int shape, int ntiles, int nact, int* warps, int* blocks, bool multi = false);
+
+// The sweep launchers of one tile shape (kernels3d_tiles.cuh; instantiated for Shape48 in
+// kernels3d.cu and for Shape84 in kernels3d_s84.cu); the functions above dispatch to them.
+template <class SH>
+struct ShapeLaunchers {
+    static pfast_status sweep(int kind, const Sweep3Args& a, int d0, int tiles, int nact, cudaStream_t st);
+    static pfast_status dataflow(int kind, const Sweep3Args& a, int nact, int maxiter, int* queue, int* result,
+                                 int warps, int blocks, cudaStream_t st);
+    static pfast_status dataflow_multi(int kind, const Sweep3Args* models, const int2* items, int nitems,
+                                       int max_ntiles, int maxiter, int* queue, int warps, int blocks, cudaStream_t st);
+    static pfast_status dataflow_shape(int kind, int ntiles, int nact, bool multi, int* warps, int* blocks);
+    static pfast_status seed(int kind, const Sweep3Args& a, int nact, cudaStream_t st);
+    static pfast_status orders(int kind, const Sweep3Args& a, int nact, cudaStream_t st);
+};
+extern template struct ShapeLaunchers<Shape48>;
+extern template struct ShapeLaunchers<Shape84>;
 
 // Small 3D kernels.
 // s64 = 1.0/vp, s32 = (float)s64 (if non-null), sq64 = s64*s64*sq_scale (if non-null); *bad is set

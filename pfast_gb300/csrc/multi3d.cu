@@ -124,14 +124,14 @@ pfast_status multi_phase(pfast_ctx* ctx, std::vector<Model>& ms, std::vector<Swe
         PFAST_CUDA_TRY(cudaMemcpyAsync(d_args, args.data(), sizeof(Sweep3Args) * nm, cudaMemcpyHostToDevice, st));
         PFAST_CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), sizeof(int2) * nitems, cudaMemcpyHostToDevice, st));
         int warps = 0, blocks = 0;
-        PFAST_TRY(dataflow_shape(kind, max_ntiles, nitems, &warps, &blocks, true));
+        PFAST_TRY(dataflow_shape(kind, 0, max_ntiles, nitems, &warps, &blocks, true));
         if (warps <= 0) {
             set_last_error("multi-model evaluation: a grid of %d tiles does not fit the dataflow kernel", max_ntiles);
             return PFAST_ERR_INVALID;
         }
         PFAST_TRY(ctx->queue.ensure(2 * sizeof(int)));
         PFAST_CUDA_TRY(cudaMemsetAsync(ctx->queue.p, 0, 2 * sizeof(int), st));
-        PFAST_LAUNCH(ctx, launch_sweep3_dataflow_multi(kind, d_args, d_items, nitems, max_ntiles, maxiter,
+        PFAST_LAUNCH(ctx, launch_sweep3_dataflow_multi(kind, 0, d_args, d_items, nitems, max_ntiles, maxiter,
                                                        ctx->queue.as<int>(), warps, blocks, st));
     }
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[1], st));

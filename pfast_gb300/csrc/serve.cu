@@ -108,7 +108,8 @@ namespace {
 void request_need(const Model& m, const Survey& s, int kind, serve::Need& n) {
     const size_t N = (size_t)m.nz * m.nr * m.nc;
     if (m.dim == 3) {
-        const size_t flags = (size_t)((m.nz + TK - 1) / TK) * ((m.nr + TI - 1) / TI) * ((m.nc + TJ - 1) / TJ) * 16;
+        // lock words of either tile shape (4x8x32, 8x4x32): at most one tile per 4x4x32 nodes
+        const size_t flags = (size_t)((m.nz + 3) / 4) * ((m.nr + 3) / 4) * ((m.nc + TJ - 1) / TJ) * 16;
         n.fixed = N * 20 + N * 8 + (size_t)s.nrec * 8 + (1u << 20);   // slowness (s, s32, s^2), output
         n.per_src = (kind == PFAST_REQ_GRADIENT ? N * 44 : N * 24) + flags + N / 8;
         n.nsrc = s.sv3->nsrc;

@@ -320,21 +320,88 @@ def test_near_source_initialisation_reduces_the_source_error(ctx):
     sv.close()
 
 
-def test_schedule_autotune(ctx):
-    """pfast_survey3d_autotune times both sweep schedules on the same evaluation; automatic
-    evaluations afterwards use the faster one and give the same bits as either forced one."""
+@pytest.mark.parametrize("shape,h", [((22, 40, 100), (20.0, 20.0, 20.0)), ((13, 17, 70), (10.0, 12.5, 8.0))])
+def test_tile_shapes_give_identical_plain_bits(ctx, shape, h):
+    """The sweeps in 4x8x32 and in 8x4x32 tiles, each per diagonal and persistent: every node
+    still sees its upstream neighbours' new values and its downstream ones' old values, so the
+    plain FP64 fields, gradients, misfits and iteration counts are bit-identical across the four
+    (schedule, tile shape) pairs and equal the oracle.  The mixed mode's FP64 polish selects
+    sweep orders per tile, so its bits may differ between shapes (not between the schedules of
+    one shape) but stay within the mixed-mode tolerances of the oracle."""
     import torch
+    from oracle import port
+    pg = _pg()
+    vp, src, srnum, rec, nxyz, tobs, Ts = _oracle_case(shape, h, 32)
+    nz, nr, nc = shape
+    sv = pg.Survey3D(ctx, nr, nc, nz, *h, src, srnum, rec, nxyz, tobs)
+    d_vp = torch.from_numpy(vp).cuda()
+    g0, e0, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h, nthreads=8)
+    picks0 = port.forward3d(vp, src, srnum, rec, 100, *h, nthreads=8)
+    out = {}
+    for prec in (pg.PFAST_PLAIN_FP64, pg.PFAST_MIXED):
+        for tile in (pg._capi.PFAST_TILE_4x8x32, pg._capi.PFAST_TILE_8x4x32):
+            for sched in (pg._capi.PFAST_SCHEDULE_DIAGONAL, pg._capi.PFAST_SCHEDULE_PERSISTENT):
+                g, e, st = sv.eval(d_vp, precision=prec, schedule=sched, tile_shape=tile)
+                pk, _ = sv.forward(d_vp, precision=prec, schedule=sched, tile_shape=tile)
+                out[prec, tile, sched] = (g.cpu().numpy(), e, pk.cpu().numpy(), st)
+                assert st["not_converged"] == 0
+    plain = [v for k, v in out.items() if k[0] == pg.PFAST_PLAIN_FP64]
+    for g, e, pk, st in plain:
+        assert bits_equal(g, g0) and e == e0 and bits_equal(pk, picks0)
+        for k in ("fwd_iters_max", "adj_iters_max"):
+            assert st[k] == plain[0][3][k], k
+    for tile in (1, 2):
+        a, b = out[pg.PFAST_MIXED, tile, 1], out[pg.PFAST_MIXED, tile, 2]
+        assert bits_equal(a[0], b[0]) and a[1] == b[1] and bits_equal(a[2], b[2])
+        assert np.linalg.norm(a[0] - g0) / np.linalg.norm(g0) <= GRAD_REL_L2_TOL
+        assert np.max(np.abs(a[2] - picks0) / np.maximum(picks0, 1e-30)) <= TT_REL_TOL   # a receiver at a source: 0
+        assert abs(a[1] - e0) <= 1e-6 * abs(e0)
+    with pytest.raises(pg.PfastError) as ei:
+        sv.eval(d_vp, tile_shape=3)
+    assert ei.value.status == pg._capi.PFAST_ERR_INVALID
+    sv.close()
+
+
+def test_dataflow_alternating_grid_sizes(ctx):
+    """The dataflow kernel's shared memory grows with the grid's tile count; a larger grid's
+    launch after a smaller grid's (launch shapes cached per grid and source count) still runs."""
+    import torch
+    pg = _pg()
+    out = []
+    for shape in ((22, 40, 100), (9, 11, 13), (22, 40, 100)):
+        h = (20.0, 20.0, 20.0)
+        vp, src, srnum, rec, nxyz, noise = case3d(shape, h, 51)
+        sv = pg.Survey3D(ctx, shape[1], shape[2], shape[0], *h, src[:2], srnum[:2], rec[:int(srnum[:2].sum())],
+                         nxyz[:int(srnum[:2].sum())], 0.2 + noise[:int(srnum[:2].sum())])
+        g, e, st = sv.eval(torch.from_numpy(vp).cuda(), precision=pg.PFAST_MIXED, schedule=2)
+        out.append((g.cpu().numpy(), e))
+        sv.close()
+    assert bits_equal(out[0][0], out[2][0]) and out[0][1] == out[2][1]
+
+
+def test_schedule_autotune(ctx):
+    """pfast_survey3d_autotune times the four (schedule, tile shape) candidates on the same
+    evaluation; automatic evaluations afterwards use the fastest per phase: plain FP64 stays
+    bit-identical to the oracle and the mixed mode within its tolerances."""
+    import torch
+    from oracle import port
     pg = _pg()
     h = (10.0, 10.0, 10.0)
     vp, src, srnum, rec, nxyz, noise = case3d((12, 16, 20), h, 41)
     tobs = 0.2 + noise
     sv = pg.Survey3D(ctx, 16, 20, 12, *h, src, srnum, rec, nxyz, tobs)
     d_vp = torch.from_numpy(vp).cuda()
-    t = sv.autotune(d_vp, precision=pg.PFAST_MIXED)
-    assert t["diagonal"]["ms_total"] > 0 and t["persistent"]["ms_total"] > 0
-    g_auto, e_auto, _ = sv.eval(d_vp, precision=pg.PFAST_MIXED)
-    g_diag, e_diag, _ = sv.eval(d_vp, precision=pg.PFAST_MIXED, schedule=pg._capi.PFAST_SCHEDULE_DIAGONAL)
-    assert bits_equal(g_auto.cpu().numpy(), g_diag.cpu().numpy()) and e_auto == e_diag
+    g0, e0, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h, nthreads=8)
+    for prec in (pg.PFAST_PLAIN_FP64, pg.PFAST_MIXED):
+        t = sv.autotune(d_vp, precision=prec)
+        assert set(t) == set(pg._capi.PFAST_TUNE_CANDIDATES)
+        assert all(v["ms_total"] > 0 for v in t.values())
+        g, e, st = sv.eval(d_vp, precision=prec)
+        g = g.cpu().numpy()
+        if prec == pg.PFAST_PLAIN_FP64:
+            assert bits_equal(g, g0) and e == e0
+        else:
+            assert np.linalg.norm(g - g0) / np.linalg.norm(g0) <= GRAD_REL_L2_TOL and st["not_converged"] == 0
     sv.close()
 
 
