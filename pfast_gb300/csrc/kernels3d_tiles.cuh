@@ -566,7 +566,7 @@ __device__ __forceinline__ unsigned adj_orders(long long t, long long xlo, long 
 // ----------------------------------------------------------- dependency-aware marking
 // Ordered integer of a value >= 0 (its bit pattern), for FP32 and FP64 fields.
 __device__ __forceinline__ long long obits(double x) { return __double_as_longlong(x); }
-__device__ __forceinline__ long long obits(float x) { return __float_as_int(x); }
+__device__ __forceinline__ int obits(float x) { return __float_as_int(x); }
 
 // ----------------------------------------------------------- the sweep kernel
 // Tile locking: a tile whose processing changed no bit of its field, and none of
@@ -891,7 +891,7 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                     // does the neighbour across a face (value vn, traveltime tn) depend on this node?
                     // The neighbour values were read before this step's stores, none of which
                     // touches them (they lie on the hyperplanes t - 1 and t + 1).
-                    const long long lo = min(obits(old), obits(nv));
+                    const auto lo = min(obits(old), obits(nv));
                     auto dep = [&](Real vn, Aux tn) {
                         if constexpr (ADJ) return obits(t0) > obits(tn);
                         else return lo < obits(vn);
