@@ -346,13 +346,16 @@ def main():
     alg_bytes = upd_dom * 3 * w                       # read U + read slowness/T + write U per node update
     iters_dom = {"fwd32": st["fwd32_iters_max"], "fwd64": st["fwd_iters_max"], "adj32": st["adj32_iters_max"],
                  "adj64": st["adj_iters_max"]}[dom]
+    tk, ti, tj = (int(x) for x in tshape.split("x"))
+    ndiag = -(-NZ // tk) + -(-NR // ti) + -(-NC // tj) - 2   # tile diagonals: nbk + nbi + nbj - 2
     if sched == "persistent":   # one dataflow launch per phase and batch
         kname = f"sweep3d_dataflow<{kind_name}, {tshape}>"
         launches_dom = st["batches"]
-    else:   # outer iterations x 8 sweep orders x tile diagonals (nbk + nbi + nbj - 2)
+    elif sched == "hybrid":   # the first outer iteration per diagonal, then one dataflow launch
+        kname = f"sweep3d_kernel + sweep3d_dataflow<{kind_name}, {tshape}>"
+        launches_dom = (8 * ndiag + 1) * st["batches"]
+    else:   # outer iterations x 8 sweep orders x tile diagonals
         kname = f"sweep3d_kernel<{kind_name}, {tshape}>"
-        tk, ti, tj = (int(x) for x in tshape.split("x"))
-        ndiag = -(-NZ // tk) + -(-NR // ti) + -(-NC // tj) - 2
         launches_dom = iters_dom * 8 * ndiag * st["batches"]
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (ms_dom / 1e3) / 1e9 if ms_dom > 0 else 0.0

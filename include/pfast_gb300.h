@@ -56,7 +56,9 @@ typedef struct {
                              per tile diagonal (every tile of every source spread over all SMs), 2 =
                              persistent: one dataflow launch per phase, one block solves one source
                              with its sweep orders overlapping as the tile dependencies allow (grids
-                             of at most 8192 tiles; larger grids use 1).  Same results. */
+                             of at most 8192 tiles; larger grids use 1), 3 = hybrid: the first outer
+                             iteration per tile diagonal, the rest in the dataflow kernel.  Same
+                             results. */
     int near_source_radius;  /* 3D forward, opt-in (not in the reference): nodes within this many grid
                              nodes of the source (Euclidean, in nodes) start from the straight-ray
                              traveltime 0.5*(s_src + s_node)*distance and stay fixed, which removes most
@@ -71,11 +73,12 @@ typedef struct {
 #define PFAST_SCHEDULE_AUTO 0
 #define PFAST_SCHEDULE_DIAGONAL 1
 #define PFAST_SCHEDULE_PERSISTENT 2
+#define PFAST_SCHEDULE_HYBRID 3
 #define PFAST_TILE_AUTO 0
 #define PFAST_TILE_4x8x32 1
 #define PFAST_TILE_8x4x32 2
 /* Candidates of the autotuner: (schedule, tile shape) pairs, index = 2*(schedule-1) + (shape-1). */
-#define PFAST_TUNE_CANDIDATES 4
+#define PFAST_TUNE_CANDIDATES 6
 
 typedef struct {
     long long fwd_node_updates;   /* executed node updates, forward sweeps (all precisions) */
@@ -161,7 +164,8 @@ pfast_status pfast_survey3d_forward(pfast_ctx* ctx, pfast_survey3d* sv, const do
 
 /* Schedule and tile-shape autotuner: runs the survey's evaluation (gradient when it has picks,
  * else picks) once per candidate (schedule, tile shape) -- per-diagonal 4x8x32, per-diagonal
- * 8x4x32, persistent 4x8x32, persistent 8x4x32 -- on the DEVICE model vp and records each
+ * 8x4x32, persistent 4x8x32, persistent 8x4x32, hybrid 4x8x32, hybrid 8x4x32 -- on the DEVICE
+ * model vp and records each
  * phase's time per (sweep kind, grid shape, source count); later calls with schedule and
  * tile_shape both automatic use, per phase, the fastest candidate.  stats: null, or an array of
  * PFAST_TUNE_CANDIDATES records in that order (a persistent candidate whose grid does not fit

@@ -21,10 +21,11 @@ PFAST_ERR_LINE_SEARCH = 8
 
 PFAST_PLAIN_FP64 = 0
 PFAST_MIXED = 1
-PFAST_SCHEDULE_AUTO, PFAST_SCHEDULE_DIAGONAL, PFAST_SCHEDULE_PERSISTENT = 0, 1, 2
+PFAST_SCHEDULE_AUTO, PFAST_SCHEDULE_DIAGONAL, PFAST_SCHEDULE_PERSISTENT, PFAST_SCHEDULE_HYBRID = 0, 1, 2, 3
 PFAST_TILE_AUTO, PFAST_TILE_4x8x32, PFAST_TILE_8x4x32 = 0, 1, 2
 # autotuner candidates, in the order of pfast_survey3d_autotune's stats array
-PFAST_TUNE_CANDIDATES = ("diagonal 4x8x32", "diagonal 8x4x32", "persistent 4x8x32", "persistent 8x4x32")
+PFAST_TUNE_CANDIDATES = ("diagonal 4x8x32", "diagonal 8x4x32", "persistent 4x8x32", "persistent 8x4x32",
+                         "hybrid 4x8x32", "hybrid 8x4x32")
 
 
 class Options(C.Structure):

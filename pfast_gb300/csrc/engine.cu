@@ -157,13 +157,15 @@ Spacing3 make_spacing(double dx, double dy, double dz) {
 // Run outer iterations of `kind` over the active batch instances until each one
 // converges or reaches maxiter.  iters[b] receives the iteration count of instance b.
 // Autotuner, per (device, sweep kind, grid, active instances): phase times of the candidate
-// (schedule, tile shape) pairs -- c = 2*persistent + shape -- measured by pfast_survey3d_autotune,
-// which runs the same evaluation once with each.  A phase picks, among the candidates its options
-// allow and its grid fits, the fastest one once all of them are measured; before that, the
-// dataflow kernel from two instances per SM (else one launch per tile diagonal) with 4x8x32 tiles.
+// (schedule, tile shape) pairs -- c = 2*schedule + shape, schedule 0 per diagonal, 1 dataflow,
+// 2 hybrid -- measured by pfast_survey3d_autotune, which runs the same evaluation once with
+// each.  A phase picks, among the candidates its options allow and its grid fits, the fastest
+// one once all of them are measured; before that, the dataflow kernel from two instances per SM
+// (else one launch per tile diagonal) with 4x8x32 tiles.
+constexpr int kCandidates = 6;
 struct TuneEntry {
-    double ms[4] = {0.0, 0.0, 0.0, 0.0};
-    int n[4] = {0, 0, 0, 0};
+    double ms[kCandidates] = {};
+    int n[kCandidates] = {};
 };
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int, int, int>, TuneEntry> g_tune;
@@ -174,7 +176,7 @@ static int tuned_candidate(const std::tuple<int, int, int, int, int, int>& key, 
     if (it != g_tune.end()) {
         int best = -1;
         bool all = true;
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < kCandidates; ++c) {
             if (!(allowed >> c & 1)) continue;
             if (it->second.n[c] == 0) { all = false; break; }
             const double t = it->second.ms[c] / it->second.n[c];
@@ -183,9 +185,9 @@ static int tuned_candidate(const std::tuple<int, int, int, int, int, int>& key, 
         if (all && best >= 0) return best;
     }
     const int first = std::get<5>(key) >= 2 * sms && (allowed & 0xc) ? 2 : 0;
-    for (int c = first; c < 4; ++c)
+    for (int c = first; c < kCandidates; ++c)
         if (allowed >> c & 1) return c;
-    for (int c = 0; c < 4; ++c)
+    for (int c = 0; c < kCandidates; ++c)
         if (allowed >> c & 1) return c;
     return 0;
 }
@@ -267,13 +269,14 @@ int rows_aligned_impl(const Sweep3Args& a, int kind) {
 pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::vector<int>& active, int maxiter,
                          int* iters, long long nodes_per_sweep, long long* node_updates, int* not_conv,
                          double* ms_acc) {
-    // Two schedules.  Per-diagonal launches spread every tile of every active instance over
+    // Three schedules.  Per-diagonal launches spread every tile of every active instance over
     // all SMs (one warp per tile) and suit surveys with few instances; the dataflow kernel
     // (one block solves one instance, its sweep orders overlapping as their tile dependencies
     // allow, no host round trip per iteration) suits runs with about one instance per SM or
-    // more.  Two tile shapes, 4x8x32 and 8x4x32 nodes in sweep-order axes.  Automatic: the
-    // autotuner above.  Grids whose tiles do not fit the dataflow kernel's shared memory use
-    // the per-diagonal launches.
+    // more; the hybrid runs the first, dense outer iteration per diagonal and the sparse rest
+    // in the dataflow kernel.  Two tile shapes, 4x8x32 and 8x4x32 nodes in sweep-order axes.
+    // Automatic: the autotuner above.  Grids whose tiles do not fit the dataflow kernel's
+    // shared memory use the per-diagonal launches.
     int dev = 0, sms = 1;
     PFAST_CUDA_TRY(cudaGetDevice(&dev));
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -286,14 +289,16 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
         PFAST_TRY(ctx_diag3(ctx, a.nz, a.nr, a.nc, shape, &t));
         const int ntl = t->nbk * t->nbi * t->nbj;
         if (!active.empty()) PFAST_TRY(dataflow_shape(kind, shape, ntl, (int)active.size(), &dwarps[shape], &dblocks[shape]));
-        if (ctx->schedule != PFAST_SCHEDULE_PERSISTENT) allowed |= 1u << shape;
-        if (ctx->schedule != PFAST_SCHEDULE_DIAGONAL && dwarps[shape] > 0) allowed |= 4u << shape;
+        const int sc = ctx->schedule;
+        if (sc == PFAST_SCHEDULE_AUTO || sc == PFAST_SCHEDULE_DIAGONAL) allowed |= 1u << shape;
+        if ((sc == PFAST_SCHEDULE_AUTO || sc == PFAST_SCHEDULE_PERSISTENT) && dwarps[shape] > 0) allowed |= 4u << shape;
+        if ((sc == PFAST_SCHEDULE_AUTO || sc == PFAST_SCHEDULE_HYBRID) && dwarps[shape] > 0) allowed |= 16u << shape;
     }
-    if (!allowed)   // persistent asked for, but the grid does not fit the dataflow kernel
+    if (!allowed)   // dataflow asked for, but the grid does not fit the dataflow kernel
         allowed = ctx->tile_shape == PFAST_TILE_AUTO ? 1u : 1u << (ctx->tile_shape - 1);
     const int cand = tuned_candidate(tkey, allowed, sms);
     ctx->candidates = (ctx->candidates & ~(15 << 4 * kind)) | (cand + 1) << 4 * kind;
-    const bool persistent = cand >= 2;
+    const bool persistent = cand >> 1 == 1, hybrid = cand >> 1 == 2;
     a.shape = cand & 1;
     DiagTable3* dtp = nullptr;
     PFAST_TRY(ctx_diag3(ctx, a.nz, a.nr, a.nc, a.shape, &dtp));
@@ -338,13 +343,18 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
         // initial selected orders per tile, so the first polish sweep skips unselected tiles
         if (polish) PFAST_LAUNCH(ctx, launch_polish_orders3(kind, a, nb, nact0, st));
     }
-    if (persistent && maxiter > 0) {
+    // The dataflow kernel on the active instances from outer iteration base on (iteration
+    // counts, stamps and the cap are absolute).
+    auto dataflow_solve = [&](int base) -> pfast_status {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
         PFAST_TRY(ctx->queue.ensure(2 * sizeof(int)));
         PFAST_CUDA_TRY(cudaMemsetAsync(ctx->queue.p, 0, 2 * sizeof(int), st));
-        PFAST_TRY(launch_sweep3_dataflow(kind, a, nact, maxiter, ctx->queue.as<int>(), a.changed, dwarps[a.shape],
+        Sweep3Args b = a;
+        b.iter = base;
+        b.dyn = nullptr;
+        PFAST_TRY(launch_sweep3_dataflow(kind, b, nact, maxiter, ctx->queue.as<int>(), a.changed, dwarps[a.shape],
                                          dblocks[a.shape], st));
         ++ctx->launches;
         PFAST_TRY(ctx->h_dyn.ensure(2 * sizeof(int)));
@@ -362,7 +372,9 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
             if (h_chg[id] >> 30) still.push_back(id);
         }
         active.swap(still);
-    }
+        return PFAST_OK;
+    };
+    if (persistent && maxiter > 0) PFAST_TRY(dataflow_solve(0));
     int it = 0;
     cudaGraphExec_t exec = nullptr;
     if (ctx->graphs && !persistent && maxiter > 0 && !active.empty()) {
@@ -373,7 +385,8 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
         PFAST_TRY(iteration_graph(ctx, a, kind, dt, nb, (int)active.size(), st, &exec));
         if (!exec) a.dyn = nullptr;   // launched one by one
     }
-    while (!persistent && !active.empty() && it < maxiter) {
+    const int diag_iters = hybrid ? std::min(maxiter, 1) : maxiter;   // hybrid: the first iteration
+    while (!persistent && !active.empty() && it < diag_iters) {
         const int nact = (int)active.size();
         std::memcpy(h_act, active.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
@@ -415,6 +428,7 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
         }
         active.swap(still);
     }
+    if (hybrid && !active.empty() && it < maxiter) PFAST_TRY(dataflow_solve(it));
     if (not_conv) *not_conv += (int)active.size();
     PFAST_CUDA_TRY(cudaEventRecord(ctx->ev[1], st));
     unsigned long long* hw = ctx->h_work.as<unsigned long long>();
@@ -659,7 +673,7 @@ bool valid_options_impl(const pfast_options* opt) {
         set_last_error("polish_floor must be in [0, 1e-9)");
         return false;
     }
-    if (opt->schedule < PFAST_SCHEDULE_AUTO || opt->schedule > PFAST_SCHEDULE_PERSISTENT) {
+    if (opt->schedule < PFAST_SCHEDULE_AUTO || opt->schedule > PFAST_SCHEDULE_HYBRID) {
         set_last_error("unknown schedule %d", opt->schedule);
         return false;
     }
@@ -969,7 +983,7 @@ pfast_status pfast_survey3d_autotune(pfast_ctx* ctx, pfast_survey3d* sv, const d
     ctx->tuning = true;
     pfast_status r = PFAST_OK;
     for (int c = 0; c < PFAST_TUNE_CANDIDATES && r == PFAST_OK; ++c) {
-        o.schedule = c < 2 ? PFAST_SCHEDULE_DIAGONAL : PFAST_SCHEDULE_PERSISTENT;
+        o.schedule = PFAST_SCHEDULE_DIAGONAL + c / 2;
         o.tile_shape = PFAST_TILE_4x8x32 + (c & 1);
         pfast_stats* sc = stats ? stats + c : nullptr;
         double E = 0.0;

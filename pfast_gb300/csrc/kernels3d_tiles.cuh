@@ -1048,7 +1048,8 @@ __global__ void __launch_bounds__(kWarps3 * 32) sweep3d_kernel(const Sweep3Args 
 // per-diagonal schedule, so both schedules give the same bits.  All waits are on this block's
 // own shared memory (no block waits for another) and are bounded: a block that sees no
 // progress for two seconds sets *err, records the instance as not converged and exits.
-// result[inst] = iterations | 1 << 30 when not converged.
+// result[inst] = iterations | 1 << 30 when not converged.  A.iter is the first iteration's
+// number: a solve continued from per-diagonal iterations counts on from them.
 constexpr unsigned kSlotEmpty = 0xffffffffu;
 // shared-memory copy of a model's arguments (multi-grid launches)
 constexpr int kDfArgsBytes = (int)((sizeof(Sweep3Args) + 15) / 16 * 16);
@@ -1242,7 +1243,7 @@ __global__ void __launch_bounds__(df_max_warps<KIND, SH>() * 32, 1) sweep3d_data
         const TileGrid3 g{A.nbk, A.nbi, A.nbj};
         int* diff = A.diff + (long long)inst * ntiles;
         const int* dirty = A.dirty + (long long)inst * ntiles;
-        int it = 0;
+        int it = A.iter;   // the first outer iteration (a continuation starts past 0); maxiter is absolute
         bool moved = true, aborted = false;
         while (it < maxiter) {
             // counters of orders 0 and 1, an empty ring, cleared per-tile change flags

@@ -44,8 +44,9 @@ def main():
     p.add_argument("--evals", type=int, default=1)
     p.add_argument("--picks-precision", choices=["plain", "mixed"], default="plain",
                    help="solver of the observed picks on the true model (plain FP64 by default)")
-    p.add_argument("--schedule", choices=["auto", "diagonal", "dataflow"], default="auto",
-                   help="3D sweep schedule: one launch per tile diagonal, or one dataflow launch per phase")
+    p.add_argument("--schedule", choices=["auto", "diagonal", "dataflow", "hybrid"], default="auto",
+                   help="3D sweep schedule: one launch per tile diagonal, one dataflow launch per phase, or "
+                        "the first outer iteration per diagonal and the rest in one dataflow launch")
     p.add_argument("--no-graphs", action="store_true",
                    help="launch each outer iteration's sweeps one by one instead of replaying captured graphs")
     a = p.parse_args()
@@ -62,7 +63,7 @@ def main():
     d = torch.from_numpy(v0).cuda()
     for _ in range(a.evals):
         t = time.perf_counter()
-        g, e, st = sv.eval(d, precision=prec, schedule={"auto": 0, "diagonal": 1, "dataflow": 2}[a.schedule])
+        g, e, st = sv.eval(d, precision=prec, schedule={"auto": 0, "diagonal": 1, "dataflow": 2, "hybrid": 3}[a.schedule])
         print(f"eval {time.perf_counter() - t:.3f} s misfit {e:.6g}", {k: v for k, v in st.items() if v}, flush=True)
     sv.close()
     ctx.close()

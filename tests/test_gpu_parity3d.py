@@ -213,9 +213,9 @@ def test_mixed_precision_within_tolerance(ctx):
 
 def test_persistent_schedule_matches_per_diagonal(ctx):
     """1600 sources on a 7 x 9 x 11 grid: more instances than resident blocks, so the persistent
-    kernel's queue hands out several instances per block.  Both schedules run the same ordered
-    sweeps per source: plain and mixed results are bit-identical between them, and the plain
-    ones equal the oracle's."""
+    kernel's queue hands out several instances per block.  All three schedules (per diagonal,
+    dataflow, hybrid) run the same ordered sweeps per source: plain and mixed results are
+    bit-identical between them, and the plain ones equal the oracle's."""
     import torch
     from oracle import port
     pg = _pg()
@@ -233,14 +233,15 @@ def test_persistent_schedule_matches_per_diagonal(ctx):
     d_vp = torch.from_numpy(vp).cuda()
     out = {}
     for prec in (pg.PFAST_PLAIN_FP64, pg.PFAST_MIXED):
-        for sched in (pg._capi.PFAST_SCHEDULE_DIAGONAL, pg._capi.PFAST_SCHEDULE_PERSISTENT):
+        for sched in (1, 2, 3):   # per diagonal, dataflow, hybrid
             g, e, st = sv.eval(d_vp, precision=prec, schedule=sched)
             pk, _ = sv.forward(d_vp, precision=prec, schedule=sched)
             out[prec, sched] = (g.cpu().numpy(), e, pk.cpu().numpy(), st)
     for prec in (pg.PFAST_PLAIN_FP64, pg.PFAST_MIXED):
-        a, b = out[prec, 1], out[prec, 2]
-        assert bits_equal(a[0], b[0]) and a[1] == b[1] and bits_equal(a[2], b[2])
-        assert a[3]["fwd_iters_max"] == b[3]["fwd_iters_max"] and a[3]["not_converged"] == b[3]["not_converged"] == 0
+        for sched in (2, 3):
+            a, b = out[prec, 1], out[prec, sched]
+            assert bits_equal(a[0], b[0]) and a[1] == b[1] and bits_equal(a[2], b[2])
+            assert a[3]["fwd_iters_max"] == b[3]["fwd_iters_max"] and a[3]["not_converged"] == b[3]["not_converged"] == 0
     g0, e0, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, h, h, h, nthreads=8)
     assert bits_equal(out[pg.PFAST_PLAIN_FP64, 2][0], g0) and out[pg.PFAST_PLAIN_FP64, 2][1] == e0
     sv.close()
@@ -249,7 +250,8 @@ def test_persistent_schedule_matches_per_diagonal(ctx):
 @pytest.mark.parametrize("shape,h", [((22, 40, 100), (20.0, 20.0, 20.0)), ((13, 17, 70), (10.0, 12.5, 8.0))])
 def test_dataflow_schedule_matches_per_diagonal_on_many_tiles(ctx, shape, h):
     """A grid of 6 x 5 x 4 (and 4 x 3 x 3) tiles with a few sources: in the dataflow schedule
-    one block solves a source with its sweep orders overlapping as the tile dependencies allow.
+    one block solves a source with its sweep orders overlapping as the tile dependencies allow;
+    the hybrid runs the first outer iteration per diagonal and continues in the dataflow kernel.
     Plain and mixed fields, gradients, misfits and iteration counts are bit-identical to the
     per-diagonal launches, and plain equals the oracle."""
     import torch
@@ -261,24 +263,27 @@ def test_dataflow_schedule_matches_per_diagonal_on_many_tiles(ctx, shape, h):
     d_vp = torch.from_numpy(vp).cuda()
     out = {}
     for prec in (pg.PFAST_PLAIN_FP64, pg.PFAST_MIXED):
-        for sched in (pg._capi.PFAST_SCHEDULE_DIAGONAL, pg._capi.PFAST_SCHEDULE_PERSISTENT):
+        for sched in (1, 2, 3):   # per diagonal, dataflow, hybrid
             g, e, st = sv.eval(d_vp, precision=prec, schedule=sched)
             pk, _ = sv.forward(d_vp, precision=prec, schedule=sched)
             out[prec, sched] = (g.cpu().numpy(), e, pk.cpu().numpy(), st)
-        a, b = out[prec, 1], out[prec, 2]
-        assert bits_equal(a[0], b[0]) and a[1] == b[1] and bits_equal(a[2], b[2])
-        for k in ("fwd_iters_max", "adj_iters_max", "fwd32_iters_max", "adj32_iters_max", "fwd_node_updates",
-                  "adj_node_updates", "not_converged"):
-            assert a[3][k] == b[3][k], k
+        a = out[prec, 1]
+        for sched in (2, 3):
+            b = out[prec, sched]
+            assert bits_equal(a[0], b[0]) and a[1] == b[1] and bits_equal(a[2], b[2])
+            for k in ("fwd_iters_max", "adj_iters_max", "fwd32_iters_max", "adj32_iters_max", "fwd_node_updates",
+                      "adj_node_updates", "not_converged"):
+                assert a[3][k] == b[3][k], (sched, k)
+            assert b[3]["launches"] < a[3]["launches"] if sched == 2 else b[3]["launches"] <= a[3]["launches"]
         assert a[3]["not_converged"] == 0 and a[3]["adj32_iters_max"] < 20 and a[3]["fwd32_iters_max"] < 20
-        assert b[3]["launches"] < a[3]["launches"]
     g0, e0, _, _ = port.eval3d(vp, src, srnum, rec, nxyz, tobs, 100, *h, nthreads=8)
     assert bits_equal(out[pg.PFAST_PLAIN_FP64, 2][0], g0) and out[pg.PFAST_PLAIN_FP64, 2][1] == e0
-    # an iteration cap: both schedules stop after the same two iterations with the same fields
+    # an iteration cap: every schedule stops after the same two iterations with the same fields
     g1, e1, s1 = sv.eval(d_vp, precision=pg.PFAST_PLAIN_FP64, maxswp=2, schedule=1)
-    g2, e2, s2 = sv.eval(d_vp, precision=pg.PFAST_PLAIN_FP64, maxswp=2, schedule=2)
-    assert bits_equal(g1.cpu().numpy(), g2.cpu().numpy()) and e1 == e2
-    assert s1["not_converged"] == s2["not_converged"] and s1["fwd_iters_max"] == s2["fwd_iters_max"] <= 2
+    for sched in (2, 3):
+        g2, e2, s2 = sv.eval(d_vp, precision=pg.PFAST_PLAIN_FP64, maxswp=2, schedule=sched)
+        assert bits_equal(g1.cpu().numpy(), g2.cpu().numpy()) and e1 == e2
+        assert s1["not_converged"] == s2["not_converged"] and s1["fwd_iters_max"] == s2["fwd_iters_max"] <= 2
     sv.close()
 
 
