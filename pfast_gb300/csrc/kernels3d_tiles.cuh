@@ -53,6 +53,20 @@ __host__ __device__ constexpr bool t_windows() {
     return Traits<KIND>::adj && sizeof(typename Traits<KIND>::Aux) == 8;
 }
 
+// Whether the field itself is kept in register windows instead of a shared-memory halo box
+// (forward polish in the dataflow kernel, COHERENT).  A lane holds its pencil's new value at
+// jf-1 and old values at jf .. jf+3 (loads issued three steps ahead); the upstream lanes' new
+// values and the downstream lanes' old values come by warp shuffle, the face halo pencils from
+// owner lanes, and each changed node is stored as it is updated.  The warp then needs no shared
+// memory, so a dataflow block holds 20 (forward) or 16 (adjoint) warps instead of 11 boxes of
+// 17 KB (3D gradient workload: forward polish 167 -> 151 ms, adjoint polish 155 -> 125 ms).
+// The per-diagonal launches keep the box: with windows their forward polish ran slower
+// (159 -> 179 ms).
+template <int KIND, bool COHERENT>
+__host__ __device__ constexpr bool u_windows() {
+    return (KIND == kFwdPolish64 || KIND == kAdjPolish64) && COHERENT;
+}
+
 // Shared memory per warp: the field's halo box, plus the FP32 bulk adjoint's traveltime
 // box.  The forward's slowness is read per node through L1 (each lane walks its own row,
 // so a fetched line serves the next steps).
@@ -68,9 +82,10 @@ __host__ __device__ constexpr bool stage_slowness() {
     return KIND == kFwdFast32;
 }
 
-template <int KIND, class SH>
+template <int KIND, class SH, bool COHERENT = false>
 __host__ __device__ constexpr int warp_smem_bytes() {
     using T = Traits<KIND>;
+    if (u_windows<KIND, COHERENT>()) return 16;   // no box
     return int(SH::HK * SH::PS * sizeof(typename T::Real) +
                (T::adj && !t_windows<KIND>() ? SH::HK * SH::PS * sizeof(typename T::Aux) : 0) +
                (stage_slowness<KIND>() ? SH::TK * SH::SPS * sizeof(typename T::Aux) : 0));
@@ -650,13 +665,16 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     Real* box = reinterpret_cast<Real*>(wsm);
     Aux* aux = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
     constexpr bool TWIN = t_windows<KIND>();
+    constexpr bool UWIN = u_windows<KIND, COHERENT>();
     Real* fld = reinterpret_cast<Real*>(A.field) + inst * A.fstride;
 
     // ---- stage the field halo box (out-of-grid: +inf for the forward so that the
     // neighbour minimum reduces to the one-sided rule at faces; never read by the adjoint)
     const Real fill = ADJ ? Real(0) : Real(INFINITY);
-    if (A.vec_rows) load_box_vec<Real, COHERENT, SH>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
-    else load_box<Real, COHERENT, SH>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
+    if constexpr (!UWIN) {
+        if (A.vec_rows) load_box_vec<Real, COHERENT, SH>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
+        else load_box<Real, COHERENT, SH>(box, fld, k0, i0, j0, ek, ei, ej, pz, py, px, nz, nr, nc, fill, lane);
+    }
     Aux* stile = reinterpret_cast<Aux*>(reinterpret_cast<unsigned char*>(box) + HK * PS * sizeof(Real));
     if constexpr (stage_slowness<KIND>())
         load_interior<Aux, SH>(stile, reinterpret_cast<const Aux*>(A.aux), k0, i0, j0, ek, ei, ej, pz, py, px, nr, nc,
@@ -745,8 +763,10 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
     const Aux* Tb = TWIN ? reinterpret_cast<const Aux*>(A.aux) + inst * A.fstride : nullptr;
     const Aux* trow = (TWIN && lane_ok) ? Tb + rowbase : nullptr;
     const Aux* hrow = nullptr;
+    const Real* urow = (UWIN && lane_ok) ? fld + rowbase : nullptr;   // the field's windows (UWIN)
+    const Real* uhrow = nullptr;
     int hpos = 0;
-    if constexpr (TWIN) {
+    if constexpr (TWIN || UWIN) {
         int lkh = 0, lih = 0;
         bool own = false;
         if (lane < TI) {
@@ -762,7 +782,10 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             hpos = lo ? y : y + ei - 1;
         }
         const int gkh = k0 + lkh, gih = i0 + lih;
-        if (own && (unsigned)gkh < (unsigned)nz && (unsigned)gih < (unsigned)nr) hrow = Tb + gkh * plane + (long long)gih * nc;
+        if (own && (unsigned)gkh < (unsigned)nz && (unsigned)gih < (unsigned)nr) {
+            if constexpr (TWIN) hrow = Tb + gkh * plane + (long long)gih * nc;
+            if constexpr (UWIN) uhrow = fld + gkh * plane + (long long)gih * nc;
+        }
     }
     // traveltime of pencil row r at flipped position p, zero outside [plo, phi] or the grid
     auto tload = [&](const Aux* r, int p, int plo, int phi) -> Aux {
@@ -775,6 +798,22 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
         tm = tload(trow, jf0 - 1, -1, ej); t0 = tload(trow, jf0, -1, ej); tp = tload(trow, jf0 + 1, -1, ej);
         q1 = tload(trow, jf0 + 2, -1, ej); q2 = tload(trow, jf0 + 3, -1, ej);
         h0 = tload(hrow, -hpos, 0, ej - 1); hq1 = tload(hrow, 1 - hpos, 0, ej - 1); hq2 = tload(hrow, 2 - hpos, 0, ej - 1);
+    }
+    // field of pencil row r at flipped position p: the fill outside [plo, phi] or the grid (UWIN)
+    auto uload = [&](const Real* r, int p, int plo, int phi) -> Real {
+        const int g = j0 + (px ? p : ej - 1 - p);
+        if (r == nullptr || p < plo || p > phi || (unsigned)g >= (unsigned)nc) return fill;
+        if constexpr (COHERENT) return __ldcg(r + g);
+        else return __ldg(r + g);
+    };
+    // UWIN: um = new value at jf-1, u0 / up / uq1 / uq2 = old values at jf .. jf+3; uh*: the
+    // owned halo pencil at the consumer's position and two ahead
+    Real um = Real(0), u0 = Real(0), up = Real(0), uq1 = Real(0), uq2 = Real(0);
+    Real uh0 = Real(0), uhq1 = Real(0), uhq2 = Real(0);
+    if constexpr (UWIN) {
+        um = uload(urow, jf0 - 1, -1, ej); u0 = uload(urow, jf0, -1, ej); up = uload(urow, jf0 + 1, -1, ej);
+        uq1 = uload(urow, jf0 + 2, -1, ej); uq2 = uload(urow, jf0 + 3, -1, ej);
+        uh0 = uload(uhrow, -hpos, 0, ej - 1); uhq1 = uload(uhrow, 1 - hpos, 0, ej - 1); uhq2 = uload(uhrow, 2 - hpos, 0, ej - 1);
     }
 
 #pragma unroll 1
@@ -795,11 +834,29 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             Tyu = lif == 0 ? hil : c_; Tyd = lif == ei - 1 ? hih : d;
             Txu = tm; Txd = tp;
         }
+        // UWIN: the neighbours of this lane's node (flipped; u: upstream, new values; d:
+        // downstream, old values): lane (kf-1, if) is one position ahead and holds the new value
+        // at this jf as its um, lane (kf+1, if) one behind holds the old one as its up
+        Real wzu = Real(0), wzd = Real(0), wyu = Real(0), wyd = Real(0);
+        if constexpr (UWIN) {
+            const Real a = __shfl_sync(0xffffffffu, um, (lane - TI) & 31);
+            const Real b = __shfl_sync(0xffffffffu, up, (lane + TI) & 31);
+            const Real c_ = __shfl_sync(0xffffffffu, um, (lane - 1) & 31);
+            const Real d = __shfl_sync(0xffffffffu, up, (lane + 1) & 31);
+            const Real hkl = __shfl_sync(0xffffffffu, uh0, lif);
+            const Real hkh = __shfl_sync(0xffffffffu, uh0, TI + lif);
+            const Real hil = __shfl_sync(0xffffffffu, uh0, 2 * TI + lkf);
+            const Real hih = __shfl_sync(0xffffffffu, uh0, 2 * TI + TK + lkf);
+            wzu = lkf == 0 ? hkl : a; wzd = lkf == ek - 1 ? hkh : b;
+            wyu = lif == 0 ? hil : c_; wyd = lif == ei - 1 ? hih : d;
+        }
+        Real res = u0;   // UWIN: this lane's value at jf after the step
         if ((unsigned)ljf < (unsigned)ej) {
             const int c = cl + t;
-            const Real xu = box[c - 1], xd = box[c + 1], yu = box[c - HJ], yd = box[c + HJ];
-            const Real zu = box[c - PS], zd = box[c + PS];
-            const Real old = box[c];
+            const Real xu = UWIN ? um : box[c - 1], xd = UWIN ? up : box[c + 1];
+            const Real yu = UWIN ? wyu : box[c - HJ], yd = UWIN ? wyd : box[c + HJ];
+            const Real zu = UWIN ? wzu : box[c - PS], zd = UWIN ? wzd : box[c + PS];
+            const Real old = UWIN ? u0 : box[c];
             Real nv = old;
             float dstep = INFINITY;   // polish: the size of this node's change
             if constexpr (ADJ && !TWIN) {   // FP32 bulk: the traveltimes from the staged box
@@ -879,8 +936,10 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             Bits bo, bn;
             memcpy(&bo, &old, sizeof(Real));
             memcpy(&bn, &nv, sizeof(Real));
+            res = nv;
             if (bo != bn) {
-                box[c] = nv;
+                if constexpr (UWIN) fld[rowbase + gjA + dj * ljf] = nv;
+                else box[c] = nv;
                 chg = true;
                 if constexpr (kSelective) {
                     if (dstep > tol_step) moved = true;
@@ -917,7 +976,11 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
             tm = t0; t0 = tp; tp = q1; q1 = q2; q2 = tload(trow, t + 4 - lkf - lif, -1, ej);
             h0 = hq1; hq1 = hq2; hq2 = tload(hrow, t + 3 - hpos, 0, ej - 1);
         }
-        __syncwarp();
+        if constexpr (UWIN) {
+            um = res; u0 = up; up = uq1; uq1 = uq2; uq2 = uload(urow, t + 4 - lkf - lif, -1, ej);
+            uh0 = uhq1; uhq1 = uhq2; uhq2 = uload(uhrow, t + 3 - hpos, 0, ej - 1);
+        }
+        if constexpr (!UWIN) __syncwarp();
     }
 
     if constexpr (kSelective) {
@@ -961,9 +1024,11 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
         if (f_jhi && tj < A.nbj - 1) atomicOr(dirty + tid + 1, 0xff);
     }
 
-    // ---- write back; the FP64 kinds compare with the iteration-start snapshot
+    // ---- write back (UWIN: stored as updated); the FP64 kinds compare with the iteration-start
+    // snapshot
     if constexpr (!kSnap) {
-        if (A.vec_rows) {
+        if constexpr (UWIN) {
+        } else if (A.vec_rows) {
             store_tile_vec<Real, SH>(fld, box, k0, i0, j0, ek, ei, ej, pz, py, px, nr, nc, lane);
         } else {
 #pragma unroll 8
@@ -1187,11 +1252,15 @@ __device__ __forceinline__ void df_iteration(const Sweep3Args& A, const int inst
 
 // Warps per block of the dataflow kernel, at most: what 227 KB of shared memory holds beside
 // the counters and ring of an 8192-tile grid (24 at most), so that the register budget of a
-// thread follows the block size.
+// thread follows the block size.  The register-window kinds use no box: 20 warps for the
+// forward polish (102 registers a thread), 16 for the adjoint polish, which also keeps the
+// traveltime windows (128 registers).
 template <int KIND, class SH>
 __host__ __device__ constexpr int df_max_warps() {
-    return (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND, SH>() < 24 ? (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND, SH>()
-                                                                       : 24;
+    return u_windows<KIND, true>() ? (KIND == kAdjPolish64 ? 16 : 20)
+           : (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND, SH, true>() < 24
+               ? (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND, SH, true>()
+               : 24;
 }
 
 // MULTI: instances of several grids in one launch.  Item q of the queue is models[items[q].x]'s
@@ -1210,9 +1279,9 @@ __global__ void __launch_bounds__(df_max_warps<KIND, SH>() * 32, 1) sweep3d_data
     constexpr bool kSelective = (KIND == kFwdPolish64 || KIND == kAdjPolish64);
     const int nthr = blockDim.x, nw = nthr >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wsm = smem_raw + warp * warp_smem_bytes<KIND, SH>();
+    unsigned char* wsm = smem_raw + warp * warp_smem_bytes<KIND, SH, true>();
     // after the warps' boxes: (MULTI: the current model's arguments,) the counters, the ring
-    unsigned char* dyn = smem_raw + nw * warp_smem_bytes<KIND, SH>();
+    unsigned char* dyn = smem_raw + nw * warp_smem_bytes<KIND, SH, true>();
     Sweep3Args& s_args = *reinterpret_cast<Sweep3Args*>(dyn);
     unsigned* cnt = reinterpret_cast<unsigned*>(dyn + (MULTI ? kDfArgsBytes : 0));
     const unsigned qmask = (unsigned)qcap - 1u;
@@ -1427,13 +1496,13 @@ pfast_status dataflow_shape_k(int ntiles, int nact, bool multi, int* warps, int*
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const long long room = (long long)smem_max - 256 - (long long)dataflow_extra_bytes(ntiles, multi);
-    const int w = (int)std::min<long long>(df_max_warps<KIND, SH>(), room / warp_smem_bytes<KIND, SH>());
+    const int w = (int)std::min<long long>(df_max_warps<KIND, SH>(), room / warp_smem_bytes<KIND, SH, true>());
     if (ntiles > kDataflowMaxTiles || w < 1) {
         *warps = 0;
         *blocks = 0;
         return PFAST_OK;
     }
-    const size_t smem = (size_t)w * warp_smem_bytes<KIND, SH>() + dataflow_extra_bytes(ntiles, multi);
+    const size_t smem = (size_t)w * warp_smem_bytes<KIND, SH, true>() + dataflow_extra_bytes(ntiles, multi);
     auto fn = multi ? sweep3d_dataflow<KIND, true, SH> : sweep3d_dataflow<KIND, false, SH>;
     // the opt-in maximum (less the kernel's static shared memory), not this grid's size: a cached
     // shape of a larger grid launches later with more than a smaller grid's call would allow
@@ -1453,7 +1522,7 @@ pfast_status dataflow_shape_k(int ntiles, int nact, bool multi, int* warps, int*
 template <int KIND, class SH>
 pfast_status launch_dataflow_k(const Sweep3Args& a, int nact, int maxiter, int* queue, int* result, int warps,
                                int blocks, cudaStream_t st) {
-    const size_t smem = (size_t)warps * warp_smem_bytes<KIND, SH>() + dataflow_extra_bytes(a.ntiles, false);
+    const size_t smem = (size_t)warps * warp_smem_bytes<KIND, SH, true>() + dataflow_extra_bytes(a.ntiles, false);
     sweep3d_dataflow<KIND, false, SH><<<blocks, warps * 32, smem, st>>>(a, nullptr, nullptr, nact, maxiter, queue,
                                                                         result, dataflow_qcap(a.ntiles));
     cudaError_t e = cudaGetLastError();
@@ -1464,7 +1533,7 @@ pfast_status launch_dataflow_k(const Sweep3Args& a, int nact, int maxiter, int* 
 template <int KIND, class SH>
 pfast_status launch_dataflow_multi_k(const Sweep3Args* models, const int2* items, int nitems, int max_ntiles,
                                      int maxiter, int* queue, int warps, int blocks, cudaStream_t st) {
-    const size_t smem = (size_t)warps * warp_smem_bytes<KIND, SH>() + dataflow_extra_bytes(max_ntiles, true);
+    const size_t smem = (size_t)warps * warp_smem_bytes<KIND, SH, true>() + dataflow_extra_bytes(max_ntiles, true);
     Sweep3Args unused;
     std::memset(&unused, 0, sizeof(unused));
     sweep3d_dataflow<KIND, true, SH><<<blocks, warps * 32, smem, st>>>(unused, models, items, nitems, maxiter, queue,
