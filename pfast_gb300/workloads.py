@@ -47,6 +47,9 @@ def main():
     p.add_argument("--schedule", choices=["auto", "diagonal", "dataflow", "hybrid"], default="auto",
                    help="3D sweep schedule: one launch per tile diagonal, one dataflow launch per phase, or "
                         "the first outer iteration per diagonal and the rest in one dataflow launch")
+    p.add_argument("--autotune", action="store_true",
+                   help="time every (schedule, tile shape) candidate first, so that automatic phases use "
+                        "the fastest (as bench.py does)")
     p.add_argument("--no-graphs", action="store_true",
                    help="launch each outer iteration's sweeps one by one instead of replaying captured graphs")
     a = p.parse_args()
@@ -61,10 +64,17 @@ def main():
     tobs = observed_picks(ctx, vt, src, srnum, rec, pprec)
     sv = api.Survey3D(ctx, nr, nc, nz, H, H, H, src, srnum, rec, nxyz, tobs)
     d = torch.from_numpy(v0).cuda()
+    if a.autotune:
+        sv.autotune(d, precision=prec)
     for _ in range(a.evals):
         t = time.perf_counter()
+        # an NVTX range per evaluation, so that a profiler can select its kernels
+        # (ncu --nvtx --nvtx-include "evaluation/")
+        torch.cuda.nvtx.range_push("evaluation")
         g, e, st = sv.eval(d, precision=prec, schedule={"auto": 0, "diagonal": 1, "dataflow": 2, "hybrid": 3}[a.schedule])
-        print(f"eval {time.perf_counter() - t:.3f} s misfit {e:.6g}", {k: v for k, v in st.items() if v}, flush=True)
+        torch.cuda.nvtx.range_pop()
+        print(f"eval {time.perf_counter() - t:.3f} s misfit {e:.6g}", {k: v for k, v in st.items() if v},
+              api._capi.phase_candidates(st), flush=True)
     sv.close()
     ctx.close()
 
