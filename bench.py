@@ -362,9 +362,11 @@ def main():
     # DRAM traffic per launch of the polish kernels: the algorithmic bytes per launch times the
     # ratio of measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum, 9-source
     # case of this grid) to the algorithmic bytes of the same launches, per (phase, schedule and
-    # tile shape): forward polish over the 1680 per-diagonal launches of the phase; adjoint
-    # polish in the dataflow kernel (one launch per phase).  The excess over 1 is the halo re-read.
-    traffic_ratios = {("fwd64", "diagonal 4x8x32"): 1.09, ("adj64", "persistent 4x8x32"): 0.99}
+    # tile shape): forward polish over the 1680 per-diagonal launches of the phase (box); both
+    # polish kinds in the dataflow kernel (register windows, one launch per phase).  Above 1: the
+    # halo re-read; below 1: resident sources sharing the slowness / traveltime lines in L2.
+    traffic_ratios = {("fwd64", "diagonal 4x8x32"): 1.09, ("fwd64", "persistent 4x8x32"): 0.75,
+                      ("adj64", "persistent 4x8x32"): 0.92}
     ratio = traffic_ratios.get((dom, cand))
     traffic = alg_bytes / launches_dom * ratio if (ratio and launches_dom) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",

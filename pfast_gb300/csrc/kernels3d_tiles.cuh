@@ -1385,8 +1385,8 @@ __global__ void tile_orders_kernel(const Sweep3Args A) {
     if (!ADJ) { sk = A.src_kij[3 * inst]; si = A.src_kij[3 * inst + 1]; sj = A.src_kij[3 * inst + 2]; }
     const long long inf = dbits(INFINITY);
     unsigned m = 0;
-#pragma unroll 1
-    for (int r = 0; r < TK * TI; ++r) {
+#pragma unroll 4
+    for (int r = 0; r < TK * TI; ++r) {   // 4 rows' loads in flight together
         const int k = k0 + r / TI, i = i0 + r % TI;
         if (k >= nz || i >= nr || j >= nc) continue;
         const long long t = k * plane + (long long)i * nc + j;
@@ -1432,19 +1432,32 @@ __global__ void seed_tiles_kernel(const Sweep3Args A) {
     const Real* f = reinterpret_cast<const Real*>(A.field) + inst * A.fstride;
     const int tj = tid % A.nbj, ti = (tid / A.nbj) % A.nbi, tk = tid / (A.nbj * A.nbi);
     const int k0 = tk * TK, i0 = ti * TI, j0 = tj * TJ;
+    auto hit = [&](Real x) -> bool {
+        if constexpr (FLOORED) return dbits(fabs(x)) > dbits(thr);
+        else return ADJ ? (x != Real(0)) : (x < Real(kInf));
+    };
+    // the box's HK x HI rows of TJ + 2 columns (lanes: columns j0-1 .. j0+30, lanes 0-1 also
+    // j0+31, j0+32), in batches of 12 rows whose loads are all in flight together
+    constexpr int kRows = HK * HI, kBatch = 12;
+    static_assert(kRows % kBatch == 0, "whole batches");
+    const int ja = j0 - 1 + lane, jb = j0 + 31 + lane;
+    const bool oka = (unsigned)ja < (unsigned)nc, okb = lane < 2 && (unsigned)jb < (unsigned)nc;
     bool live = false;
+    const Real none = ADJ ? Real(0) : Real(kInf);   // a value that is not a hit
 #pragma unroll 1
-    for (int r = 0; r < HK * HI && !live; ++r) {
-        const int k = k0 - 1 + r / HI, i = i0 - 1 + r % HI;
-        if ((unsigned)k >= (unsigned)nz || (unsigned)i >= (unsigned)nr) continue;
-        const Real* row = f + k * plane + (long long)i * nc;
-        bool v = false;
-        for (int j = j0 - 1 + lane; j < j0 + TJ + 1; j += 32) {
-            if ((unsigned)j >= (unsigned)nc) continue;
-            const Real x = __ldg(row + j);
-            if constexpr (FLOORED) v |= dbits(fabs(x)) > dbits(thr);
-            else v |= ADJ ? (x != Real(0)) : (x < Real(kInf));
+    for (int r0 = 0; r0 < kRows && !live; r0 += kBatch) {
+        Real xa[kBatch], xb[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int k = k0 - 1 + (r0 + u) / HI, i = i0 - 1 + (r0 + u) % HI;
+            const bool in = (unsigned)k < (unsigned)nz && (unsigned)i < (unsigned)nr;
+            const Real* row = f + k * plane + (long long)i * nc;
+            xa[u] = in && oka ? __ldg(row + ja) : none;
+            xb[u] = in && okb ? __ldg(row + jb) : none;
         }
+        bool v = false;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) v |= hit(xa[u]) || hit(xb[u]);
         live = __any_sync(0xffffffffu, v);
     }
     if (lane == 0) A.dirty[(long long)inst * A.ntiles + tid] = live ? 0xff : 0;
