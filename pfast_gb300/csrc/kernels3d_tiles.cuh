@@ -58,7 +58,7 @@ __host__ __device__ constexpr bool t_windows() {
 // jf-1 and old values at jf .. jf+3 (loads issued three steps ahead); the upstream lanes' new
 // values and the downstream lanes' old values come by warp shuffle, the face halo pencils from
 // owner lanes, and each changed node is stored as it is updated.  The warp then needs no shared
-// memory, so a dataflow block holds 20 (forward) or 16 (adjoint) warps instead of 11 boxes of
+// memory, so a dataflow block holds 24 (forward) or 16 (adjoint) warps instead of 11 boxes of
 // 17 KB (3D gradient workload: forward polish 167 -> 151 ms, adjoint polish 155 -> 125 ms).
 // The per-diagonal launches keep the box: with windows their forward polish ran slower
 // (159 -> 179 ms).
@@ -1252,12 +1252,12 @@ __device__ __forceinline__ void df_iteration(const Sweep3Args& A, const int inst
 
 // Warps per block of the dataflow kernel, at most: what 227 KB of shared memory holds beside
 // the counters and ring of an 8192-tile grid (24 at most), so that the register budget of a
-// thread follows the block size.  The register-window kinds use no box: 20 warps for the
-// forward polish (102 registers a thread), 16 for the adjoint polish, which also keeps the
-// traveltime windows (128 registers).
+// thread follows the block size.  The register-window kinds use no box: 24 warps for the
+// forward polish (85 registers a thread; 20 warps measured 2 % slower), 16 for the adjoint
+// polish, which also keeps the traveltime windows (128 registers; 20 warps measured 3 % slower).
 template <int KIND, class SH>
 __host__ __device__ constexpr int df_max_warps() {
-    return u_windows<KIND, true>() ? (KIND == kAdjPolish64 ? 16 : 20)
+    return u_windows<KIND, true>() ? (KIND == kAdjPolish64 ? 16 : 24)
            : (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND, SH, true>() < 24
                ? (227 * 1024 - 256 - 40960) / warp_smem_bytes<KIND, SH, true>()
                : 24;
