@@ -161,19 +161,23 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 // neighbour minima sorted by min/max (values >= 0 or +inf: no NaN arises), so
 //   2 terms: x = (B + sqrt(2 sh^2 - B^2)) / 2
 //   3 terms: x = (A + B + sqrt(3 sh^2 - (A-B)^2 - A^2 - B^2)) / 3.
+// All three candidates are formed and the first admissible one selected, without branches: in a
+// wavefront step the lanes' nodes fall into different cases, so a branching form runs the
+// union of the paths with divergence bookkeeping anyway.  The selected value is the same
+// expression as in the branching form, bit for bit (candidates from unreached neighbours may
+// be inf or NaN; they are never selected).
 __device__ __forceinline__ float eik3_fast_iso(float a, float b, float c, float sh) {
     const float lo = fminf(a, b), hi = fmaxf(a, b);
     const float c0 = fminf(lo, c), mid = fmaxf(lo, c);
     const float b0 = fminf(hi, mid), a0 = fmaxf(hi, mid);
-    float q = c0 + sh;
-    if (q <= b0) return q;
+    const float q1 = c0 + sh;
     const float B = b0 - c0;
     const float D = fmaf(2.0f * sh, sh, -B * B);
-    q = (D >= 0.f) ? fmaf(0.5f, B + sqrt_approx(D), c0) : (float)kInf;
-    if (q <= a0) return q;
+    const float q2 = (D >= 0.f) ? fmaf(0.5f, B + sqrt_approx(D), c0) : (float)kInf;
     const float A = a0 - c0, AB = A - B;
     const float D3 = fmaf(3.0f * sh, sh, -fmaf(AB, AB, fmaf(A, A, B * B)));
-    return (D3 >= 0.f) ? fmaf(1.0f / 3.0f, (A + B) + sqrt_approx(D3), c0) : (float)kInf;
+    const float q3 = (D3 >= 0.f) ? fmaf(1.0f / 3.0f, (A + B) + sqrt_approx(D3), c0) : (float)kInf;
+    return q1 <= b0 ? q1 : (q2 <= a0 ? q2 : q3);
 }
 
 // FP64 polish Godunov update: one Newton step from the current value U0 on
@@ -261,8 +265,10 @@ __device__ __forceinline__ double adj3_plain(double T0, double Txp, double Txm, 
 __device__ __forceinline__ float adj3_bulk(float T0, float Ta, float Tb, float Tc, float Td, float Te, float Tf,
                                            float La, float Lb, float Lc, float Ld, float Le, float Lf, float L0,
                                            const Spacing3& sp) {
+    // a traveltime at or above INF around the node: lambda 0 (selected at the end, without a
+    // branch; the other terms may then be inf or NaN and are discarded)
     const float ti = (float)kInf;
-    if (T0 >= ti || Ta >= ti || Tb >= ti || Tc >= ti || Td >= ti || Te >= ti || Tf >= ti) return 0.f;
+    const bool unreached = fmaxf(fmaxf(fmaxf(T0, Ta), fmaxf(Tb, Tc)), fmaxf(fmaxf(Td, Te), Tf)) >= ti;
     // per axis: den = max(-e1, 0) + max(-e2, 0), num = max(e1, 0) L1 + max(e2, 0) L2
     auto pair = [&](float T1, float L1, float T2, float L2, float& d, float& n) {
         const float e1 = T1 - T0, e2 = T2 - T0;
@@ -285,7 +291,7 @@ __device__ __forceinline__ float adj3_bulk(float T0, float Ta, float Tb, float T
         num = (wx * nx + wy * ny) + wz * nz;
         r = (fabsf(den) > 1e-9f) ? __fdividef(num, den) : 0.f;
     }
-    return fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r;
+    return unreached ? 0.f : (fabsf(r - L0) <= 5.96e-8f * fabsf(L0) ? L0 : r);
 }
 
 // FP64 polish adjoint update in residual-correction form.  With mu_m = lambda_m where
