@@ -347,14 +347,15 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
     // counts, stamps and the cap are absolute).
     auto dataflow_solve = [&](int base) -> pfast_status {
         const int nact = (int)active.size();
-        // Heaviest instances first, by the previous phase's executed work: the last round of
-        // blocks then holds the lightest ones, which shortens the launch's tail.  Each block
-        // solves its instance alone, so the order changes no bit.
+        // Heaviest instances first, by the executed work of the same sweep kind's last phase
+        // (else of the previous phase): the last round of blocks then holds the lightest ones,
+        // which shortens the launch's tail.  Each block solves its instance alone, so the order
+        // changes no bit.
         std::vector<int> order(active);
-        if ((int)ctx->inst_work.size() == nb) {
-            const std::vector<unsigned long long>& w = ctx->inst_work;
+        const std::vector<unsigned long long>& w =
+            (int)ctx->inst_work_kind[kind].size() == nb ? ctx->inst_work_kind[kind] : ctx->inst_work;
+        if ((int)w.size() == nb)
             std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return w[x] > w[y]; });
-        }
         std::memcpy(h_act, order.data(), sizeof(int) * nact);
         PFAST_CUDA_TRY(cudaMemcpyAsync(const_cast<int*>(a.act), h_act, sizeof(int) * nact, cudaMemcpyHostToDevice, st));
         PFAST_TRY(ctx->queue.ensure(2 * sizeof(int)));
@@ -446,6 +447,7 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
     for (int b = 0; b < nb; ++b) upd += (long long)hw[b];
     if (node_updates) *node_updates += upd;
     ctx->inst_work.assign(hw, hw + nb);
+    ctx->inst_work_kind[kind].assign(hw, hw + nb);
     double ms = 0.0;
     add_elapsed(ctx->ev[0], ctx->ev[1], &ms);
     if (ms_acc) *ms_acc += ms;

@@ -59,9 +59,11 @@ struct pfast_ctx {
     // One outer iteration of a per-diagonal phase as an instantiated CUDA graph, keyed by the
     // sweep kind, the launch arguments and the active-instance count it was captured with.
     std::vector<std::pair<std::vector<unsigned char>, cudaGraphExec_t>> iter_graphs;
-    // executed node updates per batch instance of the latest 3D phase: the dataflow kernel takes
-    // the instances heaviest first by this estimate (longest-processing-time order)
+    // executed node updates per batch instance of the latest 3D phase, and of the latest phase
+    // of each sweep kind: the dataflow kernel takes the instances heaviest first by the same
+    // kind's last figures (else the previous phase's), a longest-processing-time order
     std::vector<unsigned long long> inst_work;
+    std::vector<unsigned long long> inst_work_kind[6];
     // keys seen once: a phase is captured the second time its key comes up, so one-off shapes
     // (uneven batches, a serving mix) do not pay for a graph they never replay
     std::vector<std::vector<unsigned char>> graph_seen;
