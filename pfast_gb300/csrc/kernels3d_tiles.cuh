@@ -180,6 +180,12 @@ __device__ __forceinline__ float eik3_fast_iso(float a, float b, float c, float 
     return q1 <= b0 ? q1 : (q2 <= a0 ? q2 : q3);
 }
 
+// narrow_trunc for 0 <= x < 2^128 (traveltime differences): no sign, no overflow clamp.
+__device__ __forceinline__ float narrow_pos(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    return hi < (897u << 20) ? 0.0f : __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
+}
+
 // FP64 polish Godunov update: one Newton step from the current value U0 on
 //   f(q) = sum_m w_m max(q - a_m, 0)^2 - s^2,
 // whose root is the Godunov value (the 1-, 2- and 3-term cases of
@@ -204,7 +210,7 @@ __device__ __forceinline__ double eik3_newton(double U0, double a, double b, dou
         f = fma(sp.inv2[0] * px, px, fma(sp.inv2[1] * py, py, fma(sp.inv2[2] * pz, pz, -s2)));
         wx = sp.wf[0]; wy = sp.wf[1]; wz = sp.wf[2];
     }
-    const float fx = narrow_trunc(px), fy = narrow_trunc(py), fz = narrow_trunc(pz);
+    const float fx = narrow_pos(px), fy = narrow_pos(py), fz = narrow_pos(pz);
     const float fp = 2.0f * (wx * fx + wy * fy + wz * fz);
     if (!(fp > 0.0f)) {
         big = true;
@@ -571,6 +577,16 @@ __device__ __forceinline__ unsigned fwd_orders(long long u, long long xlo, long 
     return m;
 }
 
+// One axis of fwd_orders together with the axis minimum the Newton step reads (the same value
+// as min_nonneg), so that the two share their bit-pattern compares.
+__device__ __forceinline__ unsigned fwd_axis(long long u, double lo, double hi, unsigned asc, unsigned desc,
+                                             double& mn) {
+    const long long bl = dbits(lo), bh = dbits(hi);
+    const bool lt = bl < bh, gt = bh < bl;
+    mn = lt ? lo : hi;
+    return u > (lt ? bl : bh) ? (lt ? asc : (gt ? desc : 0xffu)) : 0xffu;
+}
+
 // Adjoint polish: lambda at a node depends on the neighbours with a larger traveltime.
 // Where exactly one neighbour of an axis is larger, the orders that visit it first;
 // where both are (or neither), any order.
@@ -892,13 +908,14 @@ __device__ __forceinline__ void process_tile(const Sweep3Args& A, const int inst
                         // is not monotone, so without this every sweep would move every node.
                         // Integer compares of the bit patterns (values >= 0), in flipped terms: this
                         // sweep is order 7 there (every axis ascending).
-                        const unsigned m = fwd_orders(dbits(old), dbits(xu), dbits(xd), dbits(yu), dbits(yd), dbits(zu),
-                                                      dbits(zd));
+                        double mx, my, mz;
+                        const long long bo_ = dbits(old);
+                        const unsigned m = fwd_axis(bo_, xu, xd, kAscX, kDescX, mx) & fwd_axis(bo_, yu, yd, kAscY, kDescY, my) &
+                                           fwd_axis(bo_, zu, zd, kAscZ, kDescZ, mz);
                         sel |= m;
                         if (m & 0x80u) {
                             bool big = false;
-                            nv = eik3_newton(old, min_nonneg(xd, xu), min_nonneg(yd, yu), min_nonneg(zd, zu), s, A.slow64,
-                                             rowbase + gj, A.sp, A.polish_floor, big, dstep);
+                            nv = eik3_newton(old, mx, my, mz, s, A.slow64, rowbase + gj, A.sp, A.polish_floor, big, dstep);
                             restep |= big;
                         }
                     }
