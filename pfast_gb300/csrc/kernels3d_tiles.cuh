@@ -314,7 +314,11 @@ __device__ __forceinline__ double adj3_polish(double T0, double Txp, double Txm,
     if (unreached64(T0, Txp, Txm, Typ, Tym, Tzp, Tzm)) return 0.0;
     const double exp_ = Txp - T0, exm = Txm - T0, eyp = Typ - T0, eym = Tym - T0, ezp = Tzp - T0, ezm = Tzm - T0;
     auto mu = [&](double e, double L) { return __double2hiint(e) < 0 ? L0 : L; };
-    auto nf = [](double e) { return __double2hiint(e) < 0 ? -narrow_trunc(e) : 0.0f; };   // max(-e, 0)
+    auto nf = [](double e) {   // max(-e, 0), narrowed from the magnitude's bits (|e| < 2^128)
+        const int hi = __double2hiint(e);
+        const unsigned mag = (unsigned)hi & 0x7fffffffu, lo = (unsigned)__double2loint(e);
+        return hi < 0 && mag >= (897u << 20) ? __uint_as_float(((mag - (896u << 20)) << 3) | (lo >> 29)) : 0.0f;
+    };
     double r;
     float den;
     if (sp.iso) {
