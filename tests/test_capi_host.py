@@ -108,3 +108,32 @@ def test_workload_generators_load_no_cuda_library():
             "assert 'libpfast_gb300' not in maps\n" % ROOT)
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stderr[-2000:]
+
+
+def test_option_and_stats_layout_match_the_header():
+    """The ctypes mirrors of pfast_options / pfast_stats carry every field of the header's
+    structs in order, and the tuner's candidate constants agree with it."""
+    import ctypes as C
+    from pfast_gb300 import _capi
+    text = open(HEADER).read()
+    for struct, cls in (("pfast_options", _capi.Options), ("pfast_stats", _capi.Stats)):
+        body = re.search(r"typedef struct \{([^{}]*)\}\s*" + struct + ";", text).group(1)
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        fields = [f for decl in body.split(";") if decl.strip() for f in re.findall(r"(\w+)\s*(?=,|$)", decl.strip())]
+        assert fields == [name for name, _ in cls._fields_], struct
+    assert int(re.search(r"#define PFAST_TUNE_CANDIDATES (\d+)", text).group(1)) == len(_capi.PFAST_TUNE_CANDIDATES)
+    assert int(re.search(r"#define PFAST_SCHEDULE_HYBRID (\d+)", text).group(1)) == _capi.PFAST_SCHEDULE_HYBRID
+    assert int(re.search(r"#define PFAST_TILE_8x4x32 (\d+)", text).group(1)) == _capi.PFAST_TILE_8x4x32
+    assert C.sizeof(_capi.Stats) % 8 == 0
+
+
+def test_phase_candidates_decoding():
+    """pfast_stats.candidates: 4 bits per sweep kind, 1 + the candidate index, 0 = not run."""
+    from pfast_gb300 import _capi
+    # FP32 forward: per diagonal 4x8x32 (0); forward polish: persistent 4x8x32 (2); FP32 adjoint:
+    # per diagonal 8x4x32 (1); adjoint polish: hybrid 4x8x32 (4); the plain kinds not run
+    c = (0 + 1) << 4 | (2 + 1) << 8 | (1 + 1) << 16 | (4 + 1) << 20
+    got = _capi.phase_candidates({"candidates": c})
+    assert got == {"fwd32": "diagonal 4x8x32", "fwd64_polish": "persistent 4x8x32", "adj32": "diagonal 8x4x32",
+                   "adj64_polish": "hybrid 4x8x32"}
+    assert _capi.phase_candidates({"candidates": 0}) == {}

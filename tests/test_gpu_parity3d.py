@@ -403,6 +403,10 @@ def test_schedule_autotune(ctx):
         assert all(v["ms_total"] > 0 for v in t.values())
         g, e, st = sv.eval(d_vp, precision=prec)
         g = g.cpu().numpy()
+        picks = pg._capi.phase_candidates(st)   # every sweep kind that ran names a candidate
+        assert set(picks) == ({"fwd64_plain", "adj64_plain"} if prec == pg.PFAST_PLAIN_FP64 else
+                              {"fwd32", "fwd64_polish", "adj32", "adj64_polish"})
+        assert set(picks.values()) <= set(pg._capi.PFAST_TUNE_CANDIDATES)
         if prec == pg.PFAST_PLAIN_FP64:
             assert bits_equal(g, g0) and e == e0
         else:
