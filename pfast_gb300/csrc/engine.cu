@@ -15,6 +15,7 @@
 #include <cstring>
 #include <mutex>
 #include <algorithm>
+#include <thread>
 
 #include "engine.h"
 
@@ -86,7 +87,8 @@ std::vector<DevBuf*> ctx_buffers(pfast_ctx* ctx) {
     return {&ctx->s64,  &ctx->s32,  &ctx->sq64,     &ctx->T32,    &ctx->tflags,    &ctx->T64,   &ctx->L64,
             &ctx->scratch, &ctx->mask, &ctx->act,  &ctx->changed, &ctx->ee,     &ctx->need,    &ctx->misc,
             &ctx->grad_tmp, &ctx->vp_tmp, &ctx->picks_tmp, &ctx->f2a, &ctx->f2b, &ctx->f2c, &ctx->work,
-            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c, &ctx->dyn, &ctx->multi, &ctx->multi_meta};
+            &ctx->queue, &ctx->out_a, &ctx->out_b, &ctx->out_c, &ctx->dyn, &ctx->multi, &ctx->multi_meta, &ctx->sv_src, &ctx->sv_rec, &ctx->sv_nxyz,
+            &ctx->sv_tobs, &ctx->sv_last};
 }
 
 void ctx_release_buffers(pfast_ctx* ctx) {
@@ -832,9 +834,13 @@ pfast_status pfast_ctx_synchronize(pfast_ctx* ctx) {
 }
 
 // ------------------------------------------------------------------ 3D surveys
-pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz, double dx, double dy, double dz,
-                                   int nsrc, const int* src, const int* srnum, const int* rec, const double* nxyz,
-                                   const double* T_obs, pfast_survey3d** out) {
+// scratch: the device arrays are the context's reused buffers (the one-call host entries, which
+// destroy the survey before they return), copied on the context's stream; otherwise the survey
+// owns them.
+static pfast_status survey3d_create_impl(pfast_ctx* ctx, int nrows, int ncols, int nz, double dx, double dy, double dz,
+                                         int nsrc, const int* src, const int* srnum, const int* rec,
+                                         const double* nxyz, const double* T_obs, bool scratch,
+                                         pfast_survey3d** out) {
     if (!ctx || !out) { set_last_error("null context or output"); return PFAST_ERR_INVALID; }
     *out = nullptr;
     if (nrows < 2 || ncols < 2 || nz < 2) {
@@ -885,20 +891,77 @@ pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz,
     sv->has_picks = nxyz && T_obs;
     std::vector<unsigned char> last(std::max<long long>(nrec, 1), 0);
     if (sv->has_picks) {
-        std::vector<long long> keys;
-        std::vector<size_t> used;
-        for (int s = 0; s < nsrc; ++s)
-            mark_last_rows(
-                sv->h_ch0[s], sv->h_ch0[s + 1],
-                [&](int r) { return (long long)rec[3 * r + 2] * nrows * ncols + (long long)rec[3 * r] * ncols + rec[3 * r + 1]; },
-                [&](int r) { return T_obs[r] < 100; }, [&](int r) { last[r] = 1; }, keys, used);
+        // sources are independent (each marks its own rows): split them over host threads
+        auto mark_range = [&](int s0, int s1) {
+            std::vector<long long> keys;
+            std::vector<size_t> used;
+            for (int s = s0; s < s1; ++s)
+                mark_last_rows(
+                    sv->h_ch0[s], sv->h_ch0[s + 1],
+                    [&](int r) { return (long long)rec[3 * r + 2] * nrows * ncols + (long long)rec[3 * r] * ncols + rec[3 * r + 1]; },
+                    [&](int r) { return T_obs[r] < 100; }, [&](int r) { last[r] = 1; }, keys, used);
+        };
+        const int nth = (int)std::min<long long>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())),
+                                                 std::max<long long>(1, nrec / 65536));
+        if (nth <= 1 || nsrc < 2) {
+            mark_range(0, nsrc);
+        } else {
+            std::vector<std::thread> th;
+            for (int t = 0; t < nth; ++t) {
+                const int s0 = (int)((long long)nsrc * t / nth), s1 = (int)((long long)nsrc * (t + 1) / nth);
+                if (s1 > s0) th.emplace_back(mark_range, s0, s1);
+            }
+            for (auto& x : th) x.join();
+        }
+    }
+    pfast_status stt = PFAST_OK;
+    if (scratch) {
+        // the source tables in one buffer (16-byte aligned pieces), the rest in their own
+        sv->borrowed = true;
+        auto al = [](size_t b) { return (b + 15) / 16 * 16; };
+        const size_t b_kij = al(sizeof(int) * 3 * nsrc), b_lin = al(sizeof(long long) * nsrc);
+        const size_t b_ch0 = al(sizeof(int) * (nsrc + 1)), b_srn = al(sizeof(int) * nsrc);
+        stt = ctx->sv_src.ensure(std::max<size_t>(b_kij + b_lin + b_ch0 + b_srn, 16));
+        if (!stt) stt = ctx->sv_rec.ensure(std::max<size_t>(sizeof(int) * 3 * nrec, 16));
+        if (!stt) stt = ctx->sv_nxyz.ensure(std::max<size_t>(sv->has_picks ? sizeof(double) * 3 * nrec : 0, 16));
+        if (!stt) stt = ctx->sv_tobs.ensure(std::max<size_t>(sv->has_picks ? sizeof(double) * nrec : 0, 16));
+        if (!stt) stt = ctx->sv_last.ensure(std::max<size_t>(nrec, 16));
+        if (stt) { delete sv; return stt; }
+        unsigned char* base = ctx->sv_src.as<unsigned char>();
+        sv->d_src_kij = reinterpret_cast<int*>(base);
+        sv->d_src_lin = reinterpret_cast<long long*>(base + b_kij);
+        sv->d_ch0 = reinterpret_cast<int*>(base + b_kij + b_lin);
+        sv->d_srnum = reinterpret_cast<int*>(base + b_kij + b_lin + b_ch0);
+        sv->d_rec = ctx->sv_rec.as<int>();
+        sv->d_nxyz = ctx->sv_nxyz.as<double>();
+        sv->d_tobs = ctx->sv_tobs.as<double>();
+        sv->d_last = ctx->sv_last.as<unsigned char>();
+        auto cp = [&](void* dst, const void* h, size_t bytes) -> pfast_status {
+            if (bytes) PFAST_CUDA_TRY(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+            return PFAST_OK;
+        };
+        if (!stt) stt = cp(sv->d_src_kij, kij.data(), sizeof(int) * 3 * nsrc);
+        if (!stt) stt = cp(sv->d_src_lin, lin.data(), sizeof(long long) * nsrc);
+        if (!stt) stt = cp(sv->d_ch0, sv->h_ch0.data(), sizeof(int) * (nsrc + 1));
+        if (!stt) stt = cp(sv->d_srnum, srnum, sizeof(int) * nsrc);
+        if (!stt) stt = cp(sv->d_rec, rec, sizeof(int) * 3 * nrec);
+        if (!stt && sv->has_picks) stt = cp(sv->d_nxyz, nxyz, sizeof(double) * 3 * nrec);
+        if (!stt && sv->has_picks) stt = cp(sv->d_tobs, T_obs, sizeof(double) * nrec);
+        if (!stt) stt = cp(sv->d_last, last.data(), sizeof(unsigned char) * nrec);
+        // the host tables above are freed when this function returns
+        if (!stt) {
+            const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) stt = cuda_fail(e, "survey upload", __FILE__, __LINE__);
+        }
+        if (stt) { delete sv; return stt; }
+        *out = sv;
+        return PFAST_OK;
     }
     auto up = [&](void** dst, const void* h, size_t bytes) -> pfast_status {
         PFAST_CUDA_TRY(cudaMalloc(dst, std::max<size_t>(bytes, 16)));
         if (bytes) PFAST_CUDA_TRY(cudaMemcpy(*dst, h, bytes, cudaMemcpyHostToDevice));
         return PFAST_OK;
     };
-    pfast_status stt = PFAST_OK;
     if (!stt) stt = up((void**)&sv->d_src_kij, kij.data(), sizeof(int) * 3 * nsrc);
     if (!stt) stt = up((void**)&sv->d_src_lin, lin.data(), sizeof(long long) * nsrc);
     if (!stt) stt = up((void**)&sv->d_ch0, sv->h_ch0.data(), sizeof(int) * (nsrc + 1));
@@ -912,8 +975,17 @@ pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz,
     return PFAST_OK;
 }
 
+pfast_status pfast_survey3d_create(pfast_ctx* ctx, int nrows, int ncols, int nz, double dx, double dy, double dz,
+                                   int nsrc, const int* src, const int* srnum, const int* rec, const double* nxyz,
+                                   const double* T_obs, pfast_survey3d** out) {
+    return survey3d_create_impl(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nxyz, T_obs, false, out);
+}
+
+
+
 pfast_status pfast_survey3d_destroy(pfast_survey3d* sv) {
     if (!sv) return PFAST_OK;
+    if (sv->borrowed) { delete sv; return PFAST_OK; }   // the context's buffers
     for (void* p : {(void*)sv->d_src_kij, (void*)sv->d_src_lin, (void*)sv->d_ch0, (void*)sv->d_srnum, (void*)sv->d_rec,
                     (void*)sv->d_nxyz, (void*)sv->d_tobs, (void*)sv->d_last})
         if (p) cudaFree(p);
@@ -1011,7 +1083,7 @@ pfast_status pfast_eval3d(pfast_ctx* ctx, const double* vp, int nrows, int ncols
                           pfast_stats* stats) {
     if (!ctx || !vp || !grad || !nxyz || !T_obs) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
     pfast_survey3d* sv = nullptr;
-    PFAST_TRY(pfast_survey3d_create(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nxyz, T_obs, &sv));
+    PFAST_TRY(survey3d_create_impl(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nxyz, T_obs, true, &sv));
     const long long N = (long long)nrows * ncols * nz;
     pfast_status r = ctx->vp_tmp.ensure(sizeof(double) * N);
     if (!r) r = ctx->grad_tmp.ensure(sizeof(double) * N);
@@ -1034,7 +1106,7 @@ pfast_status pfast_forward3d(pfast_ctx* ctx, const double* vp, int nrows, int nc
                              const pfast_options* opt, double* picks, pfast_stats* stats) {
     if (!ctx || !vp || !picks) { set_last_error("null argument"); return PFAST_ERR_INVALID; }
     pfast_survey3d* sv = nullptr;
-    PFAST_TRY(pfast_survey3d_create(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nullptr, nullptr, &sv));
+    PFAST_TRY(survey3d_create_impl(ctx, nrows, ncols, nz, dx, dy, dz, nsrc, src, srnum, rec, nullptr, nullptr, true, &sv));
     const long long N = (long long)nrows * ncols * nz;
     pfast_status r = ctx->vp_tmp.ensure(sizeof(double) * N);
     if (!r) r = ctx->picks_tmp.ensure(sizeof(double) * std::max(sv->nrec, 1));

@@ -55,6 +55,8 @@ struct pfast_ctx {
     pfast::DevBuf dyn;                  // replayed iteration graphs: outer iteration, active instances
     pfast::DevBuf multi;                // multi-model evaluations: the models' work arrays
     pfast::DevBuf multi_meta;           // multi-model evaluations: argument table and instance list
+    // the one-call host entries' survey arrays (source tables, receiver rows, picks), reused
+    pfast::DevBuf sv_src, sv_rec, sv_nxyz, sv_tobs, sv_last;
     pfast::HostBuf h_dyn;
     // One outer iteration of a per-diagonal phase as an instantiated CUDA graph, keyed by the
     // sweep kind, the launch arguments and the active-instance count it was captured with.
@@ -95,6 +97,7 @@ struct pfast_survey3d {
     double* d_tobs = nullptr;
     unsigned char* d_last = nullptr;
     bool has_picks = false;
+    bool borrowed = false;           // device arrays are the context's scratch (one-call entries)
 };
 
 struct pfast_survey2d {
