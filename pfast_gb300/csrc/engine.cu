@@ -18,6 +18,7 @@
 #include <thread>
 
 #include "engine.h"
+#include "tune_policy.h"
 
 namespace pfast {
 
@@ -158,40 +159,16 @@ Spacing3 make_spacing(double dx, double dy, double dz) {
 
 // Run outer iterations of `kind` over the active batch instances until each one
 // converges or reaches maxiter.  iters[b] receives the iteration count of instance b.
-// Autotuner, per (device, sweep kind, grid, active instances): phase times of the candidate
-// (schedule, tile shape) pairs -- c = 2*schedule + shape, schedule 0 per diagonal, 1 dataflow,
-// 2 hybrid -- measured by pfast_survey3d_autotune, which runs the same evaluation once with
-// each.  A phase picks, among the candidates its options allow and its grid fits, the fastest
-// one once all of them are measured; before that, the dataflow kernel from two instances per SM
-// (else one launch per tile diagonal) with 4x8x32 tiles.
-constexpr int kCandidates = 6;
-struct TuneEntry {
-    double ms[kCandidates] = {};
-    int n[kCandidates] = {};
-};
+// Autotuner, per (device, sweep kind, grid, active instances): the phase times of each
+// (schedule, tile shape) candidate, measured by pfast_survey3d_autotune, which runs the same
+// evaluation once with each; the choice itself is tune_policy.h.
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int, int, int>, TuneEntry> g_tune;
 
 static int tuned_candidate(const std::tuple<int, int, int, int, int, int>& key, unsigned allowed, int sms) {
     std::lock_guard<std::mutex> g(g_tune_mu);
     auto it = g_tune.find(key);
-    if (it != g_tune.end()) {
-        int best = -1;
-        bool all = true;
-        for (int c = 0; c < kCandidates; ++c) {
-            if (!(allowed >> c & 1)) continue;
-            if (it->second.n[c] == 0) { all = false; break; }
-            const double t = it->second.ms[c] / it->second.n[c];
-            if (best < 0 || t < it->second.ms[best] / it->second.n[best]) best = c;
-        }
-        if (all && best >= 0) return best;
-    }
-    const int first = std::get<5>(key) >= 2 * sms && (allowed & 0xc) ? 2 : 0;
-    for (int c = first; c < kCandidates; ++c)
-        if (allowed >> c & 1) return c;
-    for (int c = 0; c < kCandidates; ++c)
-        if (allowed >> c & 1) return c;
-    return 0;
+    return tune_pick(it != g_tune.end() ? &it->second : nullptr, allowed, std::get<5>(key), sms);
 }
 
 static void tune_record(const std::tuple<int, int, int, int, int, int>& key, int which, double ms) {
@@ -284,20 +261,16 @@ pfast_status run_sweeps3(pfast_ctx* ctx, Sweep3Args a, int kind, int nb, std::ve
     PFAST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const auto tkey = std::make_tuple(dev, kind, a.nz, a.nr, a.nc, (int)active.size());
     int dwarps[kTileShapes] = {}, dblocks[kTileShapes] = {};
-    unsigned allowed = 0;
+    bool fits[kTileShapes] = {};
     for (int shape = 0; shape < kTileShapes; ++shape) {
         if (ctx->tile_shape != PFAST_TILE_AUTO && ctx->tile_shape - 1 != shape) continue;
         DiagTable3* t = nullptr;
         PFAST_TRY(ctx_diag3(ctx, a.nz, a.nr, a.nc, shape, &t));
         const int ntl = t->nbk * t->nbi * t->nbj;
         if (!active.empty()) PFAST_TRY(dataflow_shape(kind, shape, ntl, (int)active.size(), &dwarps[shape], &dblocks[shape]));
-        const int sc = ctx->schedule;
-        if (sc == PFAST_SCHEDULE_AUTO || sc == PFAST_SCHEDULE_DIAGONAL) allowed |= 1u << shape;
-        if ((sc == PFAST_SCHEDULE_AUTO || sc == PFAST_SCHEDULE_PERSISTENT) && dwarps[shape] > 0) allowed |= 4u << shape;
-        if ((sc == PFAST_SCHEDULE_AUTO || sc == PFAST_SCHEDULE_HYBRID) && dwarps[shape] > 0) allowed |= 16u << shape;
+        fits[shape] = dwarps[shape] > 0;
     }
-    if (!allowed)   // dataflow asked for, but the grid does not fit the dataflow kernel
-        allowed = ctx->tile_shape == PFAST_TILE_AUTO ? 1u : 1u << (ctx->tile_shape - 1);
+    const unsigned allowed = tune_allowed(ctx->schedule, ctx->tile_shape, fits);
     const int cand = tuned_candidate(tkey, allowed, sms);
     ctx->candidates = (ctx->candidates & ~(15 << 4 * kind)) | (cand + 1) << 4 * kind;
     const bool persistent = cand >> 1 == 1, hybrid = cand >> 1 == 2;

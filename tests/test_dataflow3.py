@@ -24,3 +24,21 @@ def test_dataflow_graph_and_counter_protocol(tmp_path):
     assert out.returncode == 0, out.stdout[-2000:]
     lines = out.stdout.split()
     assert "FAIL" not in out.stdout and out.stdout.count("ok ") == 27
+
+
+def test_autotuner_policy():
+    """The 3D autotuner's choice (pfast_gb300/csrc/tune_policy.h), compiled with g++ by
+    tests/native/tune_policy_check.cpp: the candidates each schedule / tile-shape option allows
+    (per diagonal when the grid does not fit the dataflow kernel), the untuned default
+    (dataflow from two sources per SM), and the fastest mean once all allowed are timed."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "tune_policy_check")
+        subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "pfast_gb300", "csrc"),
+                        os.path.join(HERE, "native", "tune_policy_check.cpp"), "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout
+    assert "FAIL" not in out.stdout and out.stdout.count("ok ") == 19
