@@ -274,11 +274,15 @@ def main():
     stats = []
     with ClockSampler(local) as clk:
         barrier()
+        # an NVTX range around the timed steps, so that a profiler can select their kernels
+        # (ncu --nvtx --nvtx-include "timed/")
+        torch.cuda.nvtx.range_push("timed")
         for k in range(args.steps):
             ev[k][0].record(stream)
             _, misfit, st = sv.eval(d_vp, grad=grad, precision=pg.PFAST_MIXED)
             ev[k][1].record(stream)
             stats.append(st)
+        torch.cuda.nvtx.range_pop()
         barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_ms = float(sum(step_ms))
